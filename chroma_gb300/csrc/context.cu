@@ -1,0 +1,476 @@
+// C-ABI lifecycle, field import and operator application (include/gbclover.h).
+#include <cmath>
+#include <cstring>
+
+#include "ctx.h"
+
+namespace gbc {
+
+void cuda_check(cudaError_t e, const char* where) {
+  if (e != cudaSuccess) throw CudaError{e, where};
+}
+
+double now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+void sync(gbc_ctx* c) { GBC_CUDA(cudaStreamSynchronize(c->stream)); }
+
+static size_t spinor_plane_bytes(int prec) { return prec == PREC_HALF ? 48 : prec == PREC_SINGLE ? 96 : 192; }
+
+static Spinor alloc_spinor(const Geom& g, int prec, int nrhs) {
+  Spinor s;
+  s.prec = prec;
+  s.nrhs = nrhs;
+  s.stride = g.stride;
+  s.rhs_bytes = spinor_plane_bytes(prec) * (size_t)g.stride;
+  GBC_CUDA(cudaMalloc(&s.v, s.rhs_bytes * nrhs));
+  if (prec == PREC_HALF) {
+    s.norm_rhs_stride = g.stride;
+    GBC_CUDA(cudaMalloc(&s.norm, sizeof(float) * g.stride * nrhs));
+  }
+  return s;
+}
+
+static void free_spinor(Spinor& s) {
+  if (s.v) cudaFree(s.v);
+  if (s.norm) cudaFree(s.norm);
+  s = Spinor{};
+}
+
+Spinor& workspace(gbc_ctx* c, int slot, int prec, int nrhs) {
+  Spinor& s = c->ws[slot];
+  if (s.v && s.prec == prec && s.nrhs >= nrhs) {
+    return s;
+  }
+  free_spinor(s);
+  s = alloc_spinor(c->g, prec, nrhs);
+  return s;
+}
+
+Spinor sub(const Spinor& s, int r0, int n) {
+  Spinor t = s;
+  t.v = (char*)s.v + (size_t)r0 * s.rhs_bytes;
+  if (s.norm) t.norm = s.norm + (size_t)r0 * s.norm_rhs_stride;
+  t.nrhs = n;
+  return t;
+}
+
+Red red(gbc_ctx* c) { return Red{c->d_partials, c->part_stride, c->d_result}; }
+
+void ensure_stage(gbc_ctx* c, int nrhs) {
+  size_t need = (size_t)nrhs * c->V * 24;
+  if (c->stage_cap >= need) return;
+  for (int i = 0; i < 2; ++i) {
+    if (c->d_stage[i]) cudaFree(c->d_stage[i]);
+    c->d_stage[i] = nullptr;
+  }
+  for (int i = 0; i < 2; ++i) GBC_CUDA(cudaMalloc(&c->d_stage[i], need * sizeof(double)));
+  c->stage_cap = need;
+}
+
+static size_t gauge_plane_bytes(int prec, int recon) {
+  int nc = recon == 18 ? 9 : 6;
+  if (prec == PREC_DOUBLE) return 16 * nc;
+  if (prec == PREC_SINGLE) return 16 * ((nc + 1) / 2);
+  return 8 * ((nc + 1) / 2);
+}
+
+static size_t clover_bytes(int prec) { return prec == PREC_DOUBLE ? 576 : prec == PREC_SINGLE ? 288 : 144; }
+
+static void free_prec(PrecFields& f) {
+  for (int p = 0; p < 2; ++p)
+    for (int m = 0; m < 4; ++m)
+      if (f.gauge[p][m]) cudaFree(f.gauge[p][m]);
+  for (int p = 0; p < 2; ++p)
+    if (f.clov[p]) cudaFree(f.clov[p]);
+  if (f.clovinv) cudaFree(f.clovinv);
+  f = PrecFields{};
+}
+
+void ensure_prec(gbc_ctx* c, int prec) {
+  PrecFields& f = c->pf[pidx(prec)];
+  if (f.ready) return;
+  if (!c->have_gauge) throw std::string("gauge field not loaded");
+  const Geom& g = c->g;
+  int recon = prec == PREC_DOUBLE ? 18 : c->opts.sloppy_reconstruct;
+  float* d_err = nullptr;
+  GBC_CUDA(cudaMalloc(&d_err, sizeof(float)));
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    free_prec(f);
+    size_t gb = gauge_plane_bytes(prec, recon) * g.stride;
+    for (int p = 0; p < 2; ++p)
+      for (int m = 0; m < 4; ++m) GBC_CUDA(cudaMalloc(&f.gauge[p][m], gb));
+    GBC_CUDA(cudaMemsetAsync(d_err, 0, sizeof(float), c->stream));
+    pack_gauge(g, c->d_links, prec, recon, f.gauge, c->link_coeff, d_err, c->stream);
+    float err = 0;
+    GBC_CUDA(cudaMemcpyAsync(&err, d_err, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    if (recon == 12 && !(err < 1e-6f)) {
+      if (c->opts.verbose)
+        fprintf(stderr, "gbclover: links are not SU(3) x boundary sign (err %g): using 18-real storage\n", err);
+      recon = 18;
+      continue;
+    }
+    break;
+  }
+  cudaFree(d_err);
+  f.recon = recon;
+  size_t cb = clover_bytes(prec) * g.stride;
+  for (int p = 0; p < 2; ++p) GBC_CUDA(cudaMalloc(&f.clov[p], cb));
+  GBC_CUDA(cudaMalloc(&f.clovinv, cb));
+  pack_clover(g, c->d_clov, prec, f.clov, 3, c->stream);
+  void* inv_planes[2] = {f.clovinv, nullptr};
+  pack_clover(g, c->d_inv, prec, inv_planes, 1, c->stream);
+  GBC_CUDA(cudaGetLastError());
+  sync(c);
+  f.ready = true;
+}
+
+void free_ctx_memory(gbc_ctx* c) {
+  for (auto& f : c->pf) free_prec(f);
+  for (auto& kv : c->ws) free_spinor(kv.second);
+  c->ws.clear();
+  double* bufs[] = {c->d_links, c->d_clov, c->d_inv, c->d_partials, c->d_result, c->d_a, c->d_b};
+  for (double* b : bufs)
+    if (b) cudaFree(b);
+  if (c->d_ca) cudaFree(c->d_ca);
+  if (c->d_cb) cudaFree(c->d_cb);
+  if (c->d_cg) cudaFree(c->d_cg);
+  for (int i = 0; i < 2; ++i)
+    if (c->d_stage[i]) cudaFree(c->d_stage[i]);
+  if (c->h_result) cudaFreeHost(c->h_result);
+  if (c->h_cg) cudaFreeHost(c->h_cg);
+  if (c->h_coef) cudaFreeHost(c->h_coef);
+}
+
+void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, const Spinor& in, const Spinor& out,
+         const Spinor* self, const void* clov, bool reduce, double twist) {
+  const PrecFields& f = c->pf[pidx(prec)];
+  HopArgs h{};
+  h.g = c->g;
+  h.out_parity = out_parity;
+  h.nrhs = in.nrhs;
+  h.in = in.v;
+  h.in_norm = in.norm;
+  h.in_rhs_bytes = in.rhs_bytes;
+  h.out = out.v;
+  h.out_norm = out.norm;
+  h.out_rhs_bytes = out.rhs_bytes;
+  if (self) {
+    h.self = self->v;
+    h.self_norm = self->norm;
+    h.self_rhs_bytes = self->rhs_bytes;
+  }
+  h.norm_rhs_stride = in.norm_rhs_stride;
+  for (int m = 0; m < 4; ++m) {
+    h.gauge_fwd[m] = f.gauge[out_parity][m];
+    h.gauge_bwd[m] = f.gauge[1 - out_parity][m];
+  }
+  h.clov = clov;
+  h.a = a;
+  h.twist = twist;
+  h.partials = c->d_partials;
+  h.part_stride = c->part_stride;
+  HopShape sh = in.nrhs >= 12 && in.nrhs % 12 == 0 ? HopShape{32, 12} : in.nrhs >= 4 ? HopShape{32, 4} : HopShape{128, 1};
+  int nb = hop_launch(prec, f.recon, mode, dag, reduce, h, sh, c->stream);
+  if (nb < 0) throw std::string("hopping kernel variant not compiled");
+  if (nb > c->part_stride) throw std::string("partials buffer too small");
+  GBC_CUDA(cudaGetLastError());
+  if (reduce) reduce_finalize(red(c), 1, in.nrhs, nb, c->stream);
+}
+
+void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, bool reduce) {
+  const PrecFields& f = c->pf[pidx(prec)];
+  // t_e = A_ee^-1 D_eo in_o ;  out_o = A_oo in_o - 1/4 D_oe t_e  (+ isign i mu gamma_5 in_o)
+  hop(c, prec, 0, HOP_CLOV, dag, 1.0, in, tmp_e, nullptr, f.clovinv, false);
+  hop(c, prec, 1, HOP_XPAY, dag, -0.25, tmp_e, out, &in, f.clov[1], reduce, c->act.twisted ? c->act.twisted_m : 0.0);
+}
+
+void apply_clover(gbc_ctx* c, int prec, int parity, bool inverse, const Spinor& in, const Spinor& out) {
+  const PrecFields& f = c->pf[pidx(prec)];
+  blas_clover(c->g, inverse ? f.clovinv : f.clov[parity], out, in, c->stream);
+  GBC_CUDA(cudaGetLastError());
+}
+
+}  // namespace gbc
+
+using namespace gbc;
+
+namespace {
+
+int fail(gbc_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+template <class F>
+int guarded(gbc_ctx* c, F&& f) {
+  try {
+    return f();
+  } catch (const CudaError& e) {
+    return fail(c, GBC_ERR_CUDA, std::string(e.where) + ": " + cudaGetErrorString(e.e));
+  } catch (const std::string& s) {
+    return fail(c, GBC_ERR_STATE, s);
+  } catch (const std::bad_alloc&) {
+    return fail(c, GBC_ERR_CUDA, "host allocation failed");
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbc_strerror(int s) {
+  switch (s) {
+    case GBC_OK: return "ok";
+    case GBC_ERR_ARGS: return "invalid argument";
+    case GBC_ERR_CUDA: return "CUDA error";
+    case GBC_ERR_NOT_CONVERGED: return "solver did not converge";
+    case GBC_ERR_BREAKDOWN: return "Krylov breakdown";
+    case GBC_ERR_NONFINITE: return "non-finite value";
+    case GBC_ERR_STATE: return "invalid call order";
+    case GBC_ERR_RECON: return "12-real reconstruction not possible";
+    case GBC_ERR_PRECOND: return "learned preconditioner unavailable";
+  }
+  return "unknown status";
+}
+
+const char* gbc_last_error(gbc_ctx* c) { return c ? c->err.c_str() : ""; }
+
+int gbc_create(gbc_ctx** out, const gbc_geom* geom, const gbc_action* act, const gbc_opts* opts) {
+  if (!out || !geom || !act) return GBC_ERR_ARGS;
+  *out = nullptr;
+  for (int m = 0; m < 4; ++m)
+    if (geom->dims[m] < 2) return GBC_ERR_ARGS;
+  if (geom->dims[0] % 2) return GBC_ERR_ARGS;
+  if (geom->t_boundary != 1 && geom->t_boundary != -1) return GBC_ERR_ARGS;
+  long V = (long)geom->dims[0] * geom->dims[1] * geom->dims[2] * geom->dims[3];
+  if (V / 2 > (1L << 30)) return GBC_ERR_ARGS;
+  gbc_ctx* c = new gbc_ctx;
+  int rc = guarded(c, [&]() {
+    for (int m = 0; m < 4; ++m) c->dims[m] = geom->dims[m];
+    c->V = V;
+    Geom& g = c->g;
+    for (int m = 0; m < 4; ++m) g.L[m] = geom->dims[m];
+    g.Lxh = g.L[0] / 2;
+    g.Vh = (int)(V / 2);
+    g.stride = (g.Vh + 63) / 64 * 64;
+    g.t_sign = geom->t_boundary;
+    c->act = *act;
+    gbc_opts d{GBC_PREC_HALF, GBC_RECON_12, 12, 0};
+    c->opts = opts ? *opts : d;
+    if (c->opts.sloppy_precision != GBC_PREC_HALF && c->opts.sloppy_precision != GBC_PREC_SINGLE &&
+        c->opts.sloppy_precision != GBC_PREC_DOUBLE)
+      c->opts.sloppy_precision = GBC_PREC_HALF;
+    if (c->opts.sloppy_reconstruct != 12 && c->opts.sloppy_reconstruct != 18) c->opts.sloppy_reconstruct = 12;
+    c->max_rhs = c->opts.max_rhs > 0 ? c->opts.max_rhs : 12;
+    if (c->max_rhs > 32) throw std::string("max_rhs above 32");
+    if (act->aniso) {
+      for (int m = 0; m < 4; ++m)
+        if (m != act->t_dir) c->link_coeff[m] = act->nu / act->xi_0;
+    }
+    GBC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    // reduction partials: the largest grid is the hopping kernel with 32 sites per block
+    c->part_stride = (g.Vh + 31) / 32;
+    if (c->part_stride < blas_blocks(g)) c->part_stride = blas_blocks(g);
+    GBC_CUDA(cudaMalloc(&c->d_partials, sizeof(double) * 3 * c->max_rhs * (size_t)c->part_stride));
+    GBC_CUDA(cudaMalloc(&c->d_result, sizeof(double) * 3 * c->max_rhs));
+    GBC_CUDA(cudaMallocHost(&c->h_result, sizeof(double) * 3 * c->max_rhs));
+    GBC_CUDA(cudaMalloc(&c->d_cg, sizeof(CGScalars) * c->max_rhs));
+    GBC_CUDA(cudaMallocHost(&c->h_cg, sizeof(CGScalars) * c->max_rhs));
+    GBC_CUDA(cudaMalloc(&c->d_a, sizeof(double) * c->max_rhs));
+    GBC_CUDA(cudaMalloc(&c->d_b, sizeof(double) * c->max_rhs));
+    GBC_CUDA(cudaMalloc(&c->d_ca, sizeof(double2) * c->max_rhs));
+    GBC_CUDA(cudaMalloc(&c->d_cb, sizeof(double2) * c->max_rhs));
+    GBC_CUDA(cudaMallocHost(&c->h_coef, sizeof(double2) * 2 * c->max_rhs));
+    GBC_CUDA(cudaMalloc(&c->d_links, sizeof(double) * 36 * V));
+    GBC_CUDA(cudaMalloc(&c->d_clov, sizeof(double) * 72 * V));
+    GBC_CUDA(cudaMalloc(&c->d_inv, sizeof(double) * 72 * V));
+    return GBC_OK;
+  });
+  if (rc != GBC_OK) {
+    free_ctx_memory(c);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return GBC_OK;
+}
+
+void gbc_destroy(gbc_ctx* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_ctx_memory(c);
+  precond_free(c);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+static int rebuild_from_clover(gbc_ctx* c) {
+  for (auto& f : c->pf) free_prec(f);
+  c->have_gauge = true;
+  return GBC_OK;
+}
+
+int gbc_load_gauge(gbc_ctx* c, const double* links) {
+  if (!c || !links) return GBC_ERR_ARGS;
+  return guarded(c, [&]() {
+    const long V = c->V;
+    GBC_CUDA(cudaMemcpyAsync(c->d_links, links, sizeof(double) * 36 * V, cudaMemcpyHostToDevice, c->stream));
+    const gbc_action& a = c->act;
+    CloverCoeffs cc{};
+    double ffR = a.aniso ? 1.0 / a.xi_0 : 1.0;
+    double cR = a.clov_coeff_r * 0.5 * ffR, cT = a.clov_coeff_t * 0.5;
+    double ffm = a.aniso ? a.nu / a.xi_0 : 1.0;
+    cc.diag_mass = 1.0 + 3.0 * ffm + a.mass;
+    const int pairs[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+    for (int k = 0; k < 6; ++k) {
+      bool t = a.aniso && (pairs[k][0] == a.t_dir || pairs[k][1] == a.t_dir);
+      cc.coef[k] = a.aniso ? (t ? cT : cR) : cR;
+    }
+    double* d_logdet = nullptr;
+    int* d_nneg = nullptr;
+    GBC_CUDA(cudaMalloc(&d_logdet, sizeof(double) * V));
+    GBC_CUDA(cudaMalloc(&d_nneg, sizeof(int) * V));
+    clover_build(c->dims, c->d_links, cc, c->d_clov, c->d_inv, d_logdet, d_nneg, 0, c->stream);
+    GBC_CUDA(cudaGetLastError());
+    std::vector<double> ld(V);
+    std::vector<int> nn(V);
+    GBC_CUDA(cudaMemcpyAsync(ld.data(), d_logdet, sizeof(double) * V, cudaMemcpyDeviceToHost, c->stream));
+    GBC_CUDA(cudaMemcpyAsync(nn.data(), d_nneg, sizeof(int) * V, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    cudaFree(d_logdet);
+    cudaFree(d_nneg);
+    double s = 0;
+    int n = 0;
+    for (long i = 0; i < V; ++i) {
+      s += ld[i];
+      n += nn[i];
+    }
+    c->logdet_even = s;
+    c->nneg = n;
+    if (n && c->opts.verbose) fprintf(stderr, "gbclover: WARNING %d negative clover eigenvalues\n", n);
+    return rebuild_from_clover(c);
+  });
+}
+
+int gbc_load_clover(gbc_ctx* c, const double* clov, const double* invclov) {
+  if (!c || !clov || !invclov) return GBC_ERR_ARGS;
+  if (!c->have_gauge) return fail(c, GBC_ERR_STATE, "load the gauge field first");
+  return guarded(c, [&]() {
+    GBC_CUDA(cudaMemcpyAsync(c->d_clov, clov, sizeof(double) * 72 * c->V, cudaMemcpyHostToDevice, c->stream));
+    GBC_CUDA(cudaMemcpyAsync(c->d_inv, invclov, sizeof(double) * 72 * c->V, cudaMemcpyHostToDevice, c->stream));
+    sync(c);
+    return rebuild_from_clover(c);
+  });
+}
+
+int gbc_get_clover(gbc_ctx* c, double* clov, double* inv, double* logdet, int* nneg) {
+  if (!c) return GBC_ERR_ARGS;
+  if (!c->have_gauge) return fail(c, GBC_ERR_STATE, "load the gauge field first");
+  return guarded(c, [&]() {
+    if (clov) GBC_CUDA(cudaMemcpyAsync(clov, c->d_clov, sizeof(double) * 72 * c->V, cudaMemcpyDeviceToHost, c->stream));
+    if (inv) GBC_CUDA(cudaMemcpyAsync(inv, c->d_inv, sizeof(double) * 72 * c->V, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    if (logdet) *logdet = c->logdet_even;
+    if (nneg) *nneg = c->nneg;
+    return GBC_OK;
+  });
+}
+
+int gbc_apply(gbc_ctx* c, int op, int isign, int cb, int prec, int nrhs, double* out, const double* in) {
+  if (!c || !out || !in || nrhs < 1 || nrhs > c->max_rhs) return GBC_ERR_ARGS;
+  if (isign != 1 && isign != -1) return GBC_ERR_ARGS;
+  if (prec != GBC_PREC_DOUBLE && prec != GBC_PREC_SINGLE && prec != GBC_PREC_HALF) return GBC_ERR_ARGS;
+  if (!c->have_gauge) return fail(c, GBC_ERR_STATE, "load the gauge field first");
+  if (op < 0 || op > 5 || cb < 0 || cb > 1) return GBC_ERR_ARGS;
+  if (op == GBC_OP_CLOVINV && cb != 0) return GBC_ERR_ARGS;
+  return guarded(c, [&]() {
+    ensure_prec(c, prec);
+    ensure_stage(c, nrhs);
+    const size_t n = (size_t)nrhs * c->V * 24;
+    const size_t rs = (size_t)c->V * 24;
+    GBC_CUDA(cudaMemcpyAsync(c->d_stage[0], in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    GBC_CUDA(cudaMemcpyAsync(c->d_stage[1], out, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    const bool dag = isign < 0;
+    const PrecFields& f = c->pf[pidx(prec)];
+    Spinor a = sub(workspace(c, 100, prec, nrhs), 0, nrhs);
+    Spinor b = sub(workspace(c, 101, prec, nrhs), 0, nrhs);
+    Spinor t = sub(workspace(c, 102, prec, nrhs), 0, nrhs);
+    Spinor d = sub(workspace(c, 103, prec, nrhs), 0, nrhs);
+    switch (op) {
+      case GBC_OP_DSLASH:
+        import_spinor(c->g, c->d_stage[0], rs, 1 - cb, a, c->stream);
+        hop(c, prec, cb, HOP_PLAIN, dag, 1.0, a, b, nullptr, nullptr, false);
+        export_spinor(c->g, c->d_stage[1], rs, cb, b, c->stream);
+        break;
+      case GBC_OP_CLOVER:
+      case GBC_OP_CLOVINV:
+        import_spinor(c->g, c->d_stage[0], rs, cb, a, c->stream);
+        apply_clover(c, prec, cb, op == GBC_OP_CLOVINV, a, b);
+        export_spinor(c->g, c->d_stage[1], rs, cb, b, c->stream);
+        break;
+      case GBC_OP_MEO:
+      case GBC_OP_MDAGM:
+        import_spinor(c->g, c->d_stage[0], rs, 1, a, c->stream);
+        if (op == GBC_OP_MEO) {
+          apply_meo(c, prec, dag, a, b, t, false);
+        } else {
+          apply_meo(c, prec, false, a, d, t, false);
+          apply_meo(c, prec, true, d, b, t, false);
+        }
+        export_spinor(c->g, c->d_stage[1], rs, 1, b, c->stream);
+        break;
+      case GBC_OP_UNPREC: {
+        // chi_e = A_ee psi_e - 1/2 D_eo psi_o ;  chi_o = A_oo psi_o - 1/2 D_oe psi_e
+        import_spinor(c->g, c->d_stage[0], rs, 0, a, c->stream);
+        import_spinor(c->g, c->d_stage[0], rs, 1, b, c->stream);
+        hop(c, prec, 0, HOP_XPAY, dag, -0.5, b, t, &a, f.clov[0], false);
+        hop(c, prec, 1, HOP_XPAY, dag, -0.5, a, d, &b, f.clov[1], false);
+        export_spinor(c->g, c->d_stage[1], rs, 0, t, c->stream);
+        export_spinor(c->g, c->d_stage[1], rs, 1, d, c->stream);
+        break;
+      }
+    }
+    GBC_CUDA(cudaGetLastError());
+    GBC_CUDA(cudaMemcpyAsync(out, c->d_stage[1], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    return GBC_OK;
+  });
+}
+
+int gbc_solve(gbc_ctx* c, const gbc_solve_params* p, int nrhs, double* psi, const double* chi, gbc_result* res) {
+  if (!c || !p || !psi || !chi || !res || nrhs < 1 || nrhs > c->max_rhs) return GBC_ERR_ARGS;
+  if (!c->have_gauge) return fail(c, GBC_ERR_STATE, "load the gauge field first");
+  return guarded(c, [&]() {
+    double t0 = now();
+    ensure_stage(c, nrhs);
+    const size_t n = (size_t)nrhs * c->V * 24;
+    GBC_CUDA(cudaMemcpyAsync(c->d_stage[0], chi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    GBC_CUDA(cudaMemcpyAsync(c->d_stage[1], psi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    int rc = solve_device(c, p, nrhs, c->d_stage[1], c->d_stage[0], res);
+    GBC_CUDA(cudaMemcpyAsync(psi, c->d_stage[1], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    double t1 = now();
+    for (int r = 0; r < nrhs; ++r) res[r].seconds = t1 - t0;
+    return rc;
+  });
+}
+
+int gbc_solve_device(gbc_ctx* c, const gbc_solve_params* p, int nrhs, double* psi_dev, const double* chi_dev,
+                     gbc_result* res) {
+  if (!c || !p || !psi_dev || !chi_dev || !res || nrhs < 1 || nrhs > c->max_rhs) return GBC_ERR_ARGS;
+  if (!c->have_gauge) return fail(c, GBC_ERR_STATE, "load the gauge field first");
+  return guarded(c, [&]() {
+    double t0 = now();
+    int rc = solve_device(c, p, nrhs, psi_dev, chi_dev, res);
+    sync(c);
+    double t1 = now();
+    for (int r = 0; r < nrhs; ++r) res[r].seconds = t1 - t0;
+    return rc;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+// Host-side context of the C ABI: device fields, workspaces and the operator building blocks
+// shared by the solvers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/gbclover.h"
+#include "gbc_kernels.h"
+
+namespace gbc {
+
+inline int pidx(int prec) { return prec == PREC_DOUBLE ? 0 : prec == PREC_SINGLE ? 1 : 2; }
+
+struct PrecFields {
+  bool ready = false;
+  int recon = 18;
+  void* gauge[2][4] = {{nullptr}};  // [parity][mu]
+  void* clov[2] = {nullptr, nullptr};
+  void* clovinv = nullptr;  // even parity
+};
+
+struct CudaError {
+  cudaError_t e;
+  std::string where;
+};
+
+// throws CudaError on failure
+void cuda_check(cudaError_t e, const char* where);
+#define GBC_CUDA(x) ::gbc::cuda_check((x), #x)
+
+}  // namespace gbc
+
+struct gbc_ctx {
+  int dims[4];
+  long V = 0;
+  gbc::Geom g{};
+  gbc_action act{};
+  gbc_opts opts{};
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool have_gauge = false;
+  double link_coeff[4] = {1, 1, 1, 1};
+
+  // canonical FP64 copies on the device
+  double* d_links = nullptr;  // [V][36]
+  double* d_clov = nullptr;   // [V][72]
+  double* d_inv = nullptr;    // [V][72] (even sites)
+  double logdet_even = 0;
+  int nneg = 0;
+
+  gbc::PrecFields pf[3];
+
+  // reductions and CG scalars
+  int max_rhs = 12;
+  int part_stride = 0;
+  double* d_partials = nullptr;
+  double* d_result = nullptr;
+  double* h_result = nullptr;  // pinned
+  gbc::CGScalars* d_cg = nullptr;
+  gbc::CGScalars* h_cg = nullptr;  // pinned
+  double* d_a = nullptr;
+  double* d_b = nullptr;
+  double2* d_ca = nullptr;
+  double2* d_cb = nullptr;
+  double2* h_coef = nullptr;  // pinned, 2 * max_rhs
+
+  // canonical staging buffers on the device (2 x max_rhs x V x 24 doubles)
+  double* d_stage[2] = {nullptr, nullptr};
+  size_t stage_cap = 0;
+
+  // workspace spinors keyed by slot
+  std::map<int, gbc::Spinor> ws;
+
+  // learned preconditioner (opaque, owned by precond.cu)
+  void* precond = nullptr;
+};
+
+namespace gbc {
+
+// ---- workspace -----------------------------------------------------------------------------
+Spinor& workspace(gbc_ctx* c, int slot, int prec, int nrhs);
+Spinor sub(const Spinor& s, int r0, int n);  // view of right-hand sides r0..r0+n-1
+void free_ctx_memory(gbc_ctx* c);
+void ensure_prec(gbc_ctx* c, int prec);  // pack gauge/clover in this precision
+void ensure_stage(gbc_ctx* c, int nrhs);
+Red red(gbc_ctx* c);
+
+// ---- operator blocks on device fields (all of precision prec) ------------------------------
+// out(out_parity) = mode-epilogue of a * D'(in)
+void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, const Spinor& in, const Spinor& out,
+         const Spinor* self, const void* clov, bool reduce, double twist = 0.0);
+// out_o = M~ in_o (dag: M~^dag); reduce => |out|^2 in red(c).result[0][rhs]
+void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, bool reduce);
+void apply_clover(gbc_ctx* c, int prec, int parity, bool inverse, const Spinor& in, const Spinor& out);
+void sync(gbc_ctx* c);
+double now();
+
+// ---- learned preconditioner (precond.cu) ----------------------------------------------------
+void precond_free(gbc_ctx* c);
+
+// ---- solvers (solvers.cu) -------------------------------------------------------------------
+int solve_device(gbc_ctx* c, const gbc_solve_params* p, int nrhs, double* psi_canon, const double* chi_canon,
+                 gbc_result* res);
+
+}  // namespace gbc

@@ -1,0 +1,10 @@
+// Dispatch of the PrecD hopping kernels on isign.
+#include "gbc_kernels.h"
+
+namespace gbc {
+int hop_launch_d0(int recon, int mode, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+int hop_launch_d1(int recon, int mode, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+int hop_launch_d(int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
+  return dag ? hop_launch_d1(recon, mode, reduce, a, sh, s) : hop_launch_d0(recon, mode, reduce, a, sh, s);
+}
+}  // namespace gbc

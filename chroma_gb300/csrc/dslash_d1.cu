@@ -1,0 +1,9 @@
+// Hopping kernels, storage precision PrecD, isign = MINUS (dagger).
+#define GBC_RECON12 0
+#include "dslash_inst.cuh"
+
+namespace gbc {
+int hop_launch_d1(int recon, int mode, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
+  return hop_recon<PrecD, true>(recon, mode, reduce, a, sh, s);
+}
+}  // namespace gbc

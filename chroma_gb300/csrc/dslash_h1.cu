@@ -1,0 +1,9 @@
+// Hopping kernels, storage precision PrecH, isign = MINUS (dagger).
+#define GBC_RECON12 1
+#include "dslash_inst.cuh"
+
+namespace gbc {
+int hop_launch_h1(int recon, int mode, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
+  return hop_recon<PrecH, true>(recon, mode, reduce, a, sh, s);
+}
+}  // namespace gbc

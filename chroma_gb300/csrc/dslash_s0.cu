@@ -1,0 +1,9 @@
+// Hopping kernels, storage precision PrecS, isign = PLUS.
+#define GBC_RECON12 1
+#include "dslash_inst.cuh"
+
+namespace gbc {
+int hop_launch_s0(int recon, int mode, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
+  return hop_recon<PrecS, false>(recon, mode, reduce, a, sh, s);
+}
+}  // namespace gbc

@@ -1,0 +1,142 @@
+// Host-visible kernel interface of the GB300 clover solver library (internal, not the C-ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace gbc {
+
+enum { HOP_PLAIN = 0, HOP_CLOV = 1, HOP_XPAY = 2 };
+enum { PREC_HALF = 2, PREC_SINGLE = 4, PREC_DOUBLE = 8 };
+
+struct Geom {
+  int L[4];
+  int Lxh;
+  int Vh;
+  int stride;  // padded plane length (multiple of 64 sites)
+  int t_sign;  // -1 when the links at t = Lt-1 carry the antiperiodic sign (12-real reconstruction)
+};
+
+// One checkerboard spinor field holding nrhs right-hand sides in precision prec.
+struct Spinor {
+  int prec = 0;
+  int nrhs = 0;
+  int stride = 0;
+  void* v = nullptr;
+  float* norm = nullptr;        // half precision only
+  size_t rhs_bytes = 0;         // bytes between right-hand sides in v
+  size_t norm_rhs_stride = 0;   // floats between right-hand sides in norm
+};
+
+struct HopArgs {
+  Geom g;
+  int out_parity;
+  int nrhs;
+  const void* in;
+  const float* in_norm;
+  size_t in_rhs_bytes;
+  void* out;
+  float* out_norm;
+  size_t out_rhs_bytes;
+  const void* self;
+  const float* self_norm;
+  size_t self_rhs_bytes;
+  size_t norm_rhs_stride;
+  const void* gauge_fwd[4];  // links U_mu(x) of the output parity
+  const void* gauge_bwd[4];  // links U_mu(x) of the input parity (used as U_mu^dag(x - mu))
+  const void* clov;          // packed clover of the output parity (HOP_CLOV, HOP_XPAY)
+  double a;                  // coefficient of D' psi
+  double twist;              // HOP_XPAY: twisted-mass mu (0 = none)
+  double* partials;          // REDUCE: |out|^2 per block, [rhs][part_stride]
+  int part_stride;
+};
+
+// Launch geometry chosen by the caller (autotuned): TX sites x NRB right-hand sides per block.
+struct HopShape {
+  int tx;
+  int nrb;
+};
+
+// Returns the number of x-blocks launched (partials per right-hand side), or -1 if the
+// (precision, recon, shape) combination is not compiled.
+int hop_launch_d(int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+int hop_launch_s(int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+int hop_launch_h(int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+
+inline int hop_launch(int prec, int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh,
+                      cudaStream_t s) {
+  switch (prec) {
+    case PREC_DOUBLE: return hop_launch_d(recon, mode, dag, reduce, a, sh, s);
+    case PREC_SINGLE: return hop_launch_s(recon, mode, dag, reduce, a, sh, s);
+    case PREC_HALF: return hop_launch_h(recon, mode, dag, reduce, a, sh, s);
+  }
+  return -1;
+}
+
+// ---- field import / export / packing (fields.cu) ---------------------------------------------
+// canonical complex128 links [V][4][3][3] -> planes of (parity, mu) in prec/recon, links of
+// direction mu scaled by coeff[mu]; max |row2 - sign*conj(row0 x row1)| written to *recon_err.
+void pack_gauge(const Geom& g, const double* canon, int prec, int recon, void* const planes[2][4],
+                const double coeff[4], float* recon_err, cudaStream_t s);
+// canonical packed clover [V][72] -> per-parity planes (only parity p_mask bit set: 1 even, 2 odd)
+void pack_clover(const Geom& g, const double* canon, int prec, void* const planes[2], int p_mask, cudaStream_t s);
+// canonical spinor [V][12] complex128 of rhs r at canon + r*canon_rhs (doubles) <-> parity cb field
+void import_spinor(const Geom& g, const double* canon, size_t canon_rhs, int cb, const Spinor& f, cudaStream_t s);
+void export_spinor(const Geom& g, double* canon, size_t canon_rhs, int cb, const Spinor& f, cudaStream_t s);
+
+// ---- clover construction on the device (clover.cu) --------------------------------------------
+struct CloverCoeffs {
+  double diag_mass;
+  double coef[6];  // clover coefficient (with the 1/2) of the planes 01,02,03,12,13,23
+};
+// clov[V][72] = packed A (all sites); inv[V][72] = packed A^-1 on the sites of parity inv_parity
+// (zero elsewhere); logdet[V] = sum log|d_i| of the LDL^dag factors on those sites, nneg[V] the
+// number of negative d_i.
+void clover_build(const int dims[4], const double* canon_links, const CloverCoeffs& cc, double* clov, double* inv,
+                  double* logdet, int* nneg, int inv_parity, cudaStream_t s);
+void clover_invert(long nsites, double* packed, double* logdet, int* nneg, cudaStream_t s);
+
+// ---- BLAS-1 and reductions (blas.cu) ----------------------------------------------------------
+// Every vector argument is a Spinor of Vh sites and nrhs right-hand sides; coefficient arrays
+// live in device memory, one value (double) or complex (double2) per right-hand side.
+struct Red {
+  double* partials;  // [nred][nrhs][part_stride]
+  int part_stride;
+  double* result;    // [nred][nrhs]
+};
+int blas_blocks(const Geom& g);  // blocks per right-hand side of the reduction kernels
+
+void blas_copy(const Geom& g, const Spinor& y, const Spinor& x, cudaStream_t s);       // y = x (any precisions)
+void blas_zero(const Geom& g, const Spinor& y, cudaStream_t s);
+void blas_axpby(const Geom& g, const double2* a, const Spinor& x, const double2* b, const Spinor& y,
+                cudaStream_t s);                                                           // y = a x + b y
+void blas_norm2(const Geom& g, const Spinor& x, const Red& r, cudaStream_t s);             // result[0][rhs]
+void blas_cdot(const Geom& g, const Spinor& x, const Spinor& y, const Red& r, cudaStream_t s);  // <x,y> -> result[0..1]
+// CG update: x += a p;  r -= a q;  result = |r|^2      (a per rhs, real)
+void blas_cg_update(const Geom& g, const double* a, const Spinor& x, const Spinor& p, const Spinor& r,
+                    const Spinor& q, const Red& red, cudaStream_t s);
+// p = r + b p  (b per rhs, real)
+void blas_xpay(const Geom& g, const Spinor& r, const double* b, const Spinor& p, cudaStream_t s);
+// y = x - y, result = |y|^2    (residual from a source and M psi)
+void blas_xmy_norm2(const Geom& g, const Spinor& x, const Spinor& y, const Red& red, cudaStream_t s);
+// x += y (y may be lower precision)
+void blas_xpy(const Geom& g, const Spinor& x, const Spinor& y, cudaStream_t s);
+// finalize the partial sums of nred quantities x nrhs into red.result
+void reduce_finalize(const Red& red, int nred, int nrhs, int nblocks, cudaStream_t s);
+
+// ---- CG scalar control on the device (blas.cu) ------------------------------------------------
+struct CGScalars {
+  double c, d, a, b, cp, rsd_sq, c_prev;
+  int active, iters;
+};
+// after |M p|^2 is in red_d: d = red_d[r]; a = active ? c/d : 0
+void cg_alpha(CGScalars* st, const double* red_d, double* a_out, int nrhs, cudaStream_t s);
+// after |r|^2 is in red_r: cp; converged -> active = 0; b = active ? cp/c : 0; c = cp; iters++
+void cg_beta(CGScalars* st, const double* red_r, double* b_out, int nrhs, cudaStream_t s);
+
+}  // namespace gbc
+
+namespace gbc {
+// out = T in (T = packed clover blocks of the field's parity, prec of the spinors)
+void blas_clover(const Geom& g, const void* clov, const Spinor& out, const Spinor& in, cudaStream_t s);
+}  // namespace gbc

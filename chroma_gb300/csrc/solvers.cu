@@ -1,0 +1,493 @@
+// Krylov solvers on the device fields, batched over right-hand sides.
+//
+//   GBC_SOLVER_CG           LinOpSysSolverCG + InvCG2   (syssolver_linop_cg.h:57-96, invcg2.cc:70-232), FP64
+//   GBC_SOLVER_RELIABLE_CG  LinOpSysSolverReliableCGClover + RelInvCG_a
+//                           (syssolver_linop_rel_cg_clover.h:104-152, reliable_cg.cc:10-188):
+//                           FP64 reliable updates around a CG whose vectors are FP32 and whose
+//                           operator runs in the sloppy precision
+//   GBC_SOLVER_MIXED        FP64 defect correction (the RICHARDSON_MP_CLOVER_INVERTER pattern,
+//                           inv_multiprec_richardson.cc:13-107): each outer step recomputes the
+//                           FP64 residual and solves for the correction with a CGNE whose operator
+//                           and search vectors are in the sloppy precision and whose residual is
+//                           refreshed from an FP32 operator (reliable updates)
+//   GBC_SOLVER_FGMRES       FGMRES(NKrylov), NDefl = 0 (fgmres.cu)
+//
+// Every right-hand side carries its own scalars on the device (CGScalars); a converged right-hand
+// side keeps alpha = beta = 0 so that the batch can run on until the last one converges.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "ctx.h"
+
+namespace gbc {
+
+namespace {
+
+enum {
+  SLOT_X = 1, SLOT_B, SLOT_R, SLOT_P, SLOT_MP, SLOT_MMP, SLOT_TE, SLOT_T1, SLOT_T2, SLOT_TEH,
+  SLOT_XD, SLOT_BD, SLOT_RD, SLOT_TD1, SLOT_TD2, SLOT_TED, SLOT_ES, SLOT_RS, SLOT_CHIE, SLOT_PSIE, SLOT_SE,
+  SLOT_XS, SLOT_RHS
+};
+
+struct Batch {
+  int nrhs;
+  std::vector<double> v;
+};
+
+// result[0][r] -> host (synchronises)
+std::vector<double> fetch(gbc_ctx* c, int nred, int nrhs) {
+  GBC_CUDA(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(double) * nred * nrhs, cudaMemcpyDeviceToHost, c->stream));
+  sync(c);
+  return std::vector<double>(c->h_result, c->h_result + nred * nrhs);
+}
+
+std::vector<double> norm2(gbc_ctx* c, const Spinor& x) {
+  blas_norm2(c->g, x, red(c), c->stream);
+  return fetch(c, 1, x.nrhs);
+}
+
+// out = A x with A = M~ (normal = false) or M~^dag M~ (normal = true); |out|^2 not needed
+void apply_sys(gbc_ctx* c, int prec, bool normal, const Spinor& x, const Spinor& out, const Spinor& t, const Spinor& te) {
+  if (normal) {
+    apply_meo(c, prec, false, x, t, te, false);
+    apply_meo(c, prec, true, t, out, te, false);
+  } else {
+    apply_meo(c, prec, false, x, out, te, false);
+  }
+}
+
+struct CgCfg {
+  int pa, po;        // accumulator / operator precision
+  double rsd;        // relative target on the normal-equation residual
+  int maxit;
+  double delta;      // reliable-update trigger (0: none)
+  int check_every;   // host convergence checks
+};
+
+struct CgStats {
+  std::vector<int> iters;
+  std::vector<int> status;
+  int reliable = 0;
+};
+
+// CG on M~^dag M~ x = b (InvCG2 recursion) with per-right-hand-side device scalars.
+// active[r] == 0 skips right-hand side r (its x is left unchanged).
+CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b, bool zero_x,
+                  const std::vector<int>& active) {
+  const int n = x.nrhs;
+  const Geom& g = c->g;
+  cudaStream_t s = c->stream;
+  Spinor r = sub(workspace(c, SLOT_R + 100 * pidx(cfg.pa), cfg.pa, n), 0, n);
+  Spinor p = sub(workspace(c, SLOT_P + 100 * pidx(cfg.po), cfg.po, n), 0, n);
+  Spinor mp = sub(workspace(c, SLOT_MP + 100 * pidx(cfg.po), cfg.po, n), 0, n);
+  Spinor mmp = sub(workspace(c, SLOT_MMP + 100 * pidx(cfg.po), cfg.po, n), 0, n);
+  Spinor te = sub(workspace(c, SLOT_TE + 100 * pidx(cfg.po), cfg.po, n), 0, n);
+  CgStats st;
+  st.iters.assign(n, 0);
+  st.status.assign(n, GBC_OK);
+
+  auto true_residual = [&]() {
+    // r = b - A^dag A x in the accumulator precision
+    Spinor t1 = sub(workspace(c, SLOT_T1 + 100 * pidx(cfg.pa), cfg.pa, n), 0, n);
+    Spinor teh = sub(workspace(c, SLOT_TEH + 100 * pidx(cfg.pa), cfg.pa, n), 0, n);
+    apply_sys(c, cfg.pa, true, x, r, t1, teh);
+    blas_xmy_norm2(g, b, r, red(c), s);
+  };
+  if (zero_x) {
+    blas_zero(g, x, s);
+    blas_copy(g, r, b, s);
+    blas_norm2(g, r, red(c), s);
+  } else {
+    true_residual();
+  }
+  std::vector<double> rr = fetch(c, 1, n);
+  std::vector<double> bb = norm2(c, b);
+  std::vector<CGScalars> hs(n);
+  std::vector<double> maxrr(n);
+  for (int i = 0; i < n; ++i) {
+    CGScalars& q = hs[i];
+    std::memset(&q, 0, sizeof(q));
+    q.c = q.cp = rr[i];
+    q.c_prev = rr[i];
+    q.rsd_sq = cfg.rsd * cfg.rsd * bb[i];
+    q.active = active[i] && std::isfinite(rr[i]) && rr[i] > q.rsd_sq;
+    if (!std::isfinite(rr[i]) || !std::isfinite(bb[i])) st.status[i] = GBC_ERR_NONFINITE;
+    maxrr[i] = std::sqrt(rr[i]);
+  }
+  GBC_CUDA(cudaMemcpyAsync(c->d_cg, hs.data(), sizeof(CGScalars) * n, cudaMemcpyHostToDevice, s));
+  blas_copy(g, p, r, s);
+  bool any = false;
+  for (int i = 0; i < n; ++i) any |= hs[i].active != 0;
+  int k = 0;
+  for (k = 1; any && k <= cfg.maxit; ++k) {
+    apply_meo(c, cfg.po, false, p, mp, te, true);     // |mp|^2 -> result
+    cg_alpha(c->d_cg, c->d_result, c->d_a, n, s);
+    apply_meo(c, cfg.po, true, mp, mmp, te, false);
+    blas_cg_update(g, c->d_a, x, p, r, mmp, red(c), s);  // |r|^2 -> result
+    cg_beta(c->d_cg, c->d_result, c->d_b, n, s);
+    const bool check = cfg.delta > 0 || (k % cfg.check_every) == 0 || k == cfg.maxit;
+    if (check) {
+      GBC_CUDA(cudaMemcpyAsync(c->h_cg, c->d_cg, sizeof(CGScalars) * n, cudaMemcpyDeviceToHost, s));
+      sync(c);
+      any = false;
+      bool trigger = false;
+      for (int i = 0; i < n; ++i) {
+        if (!std::isfinite(c->h_cg[i].cp)) st.status[i] = GBC_ERR_NONFINITE;
+        if (!c->h_cg[i].active) continue;
+        any = true;
+        double rn = std::sqrt(c->h_cg[i].cp);
+        maxrr[i] = std::max(maxrr[i], rn);
+        if (cfg.delta > 0 && rn < cfg.delta * maxrr[i]) trigger = true;
+      }
+      if (any && trigger) {
+        // reliable update: r = b - A^dag A x from the accumulator-precision operator
+        true_residual();
+        std::vector<double> nr = fetch(c, 1, n);
+        std::memcpy(hs.data(), c->h_cg, sizeof(CGScalars) * n);
+        std::vector<double> bnew(n);
+        for (int i = 0; i < n; ++i) {
+          CGScalars& q = hs[i];
+          if (q.active) {
+            q.b = q.c_prev > 0 ? nr[i] / q.c_prev : 0.0;
+            q.c = q.cp = nr[i];
+            maxrr[i] = std::sqrt(nr[i]);
+            if (!(nr[i] > q.rsd_sq)) {
+              q.active = 0;
+              q.b = 0;
+            }
+          }
+          bnew[i] = q.b;
+        }
+        GBC_CUDA(cudaMemcpyAsync(c->d_cg, hs.data(), sizeof(CGScalars) * n, cudaMemcpyHostToDevice, s));
+        GBC_CUDA(cudaMemcpyAsync(c->d_b, bnew.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        sync(c);
+        ++st.reliable;
+      }
+      if (!any) break;
+    }
+    blas_xpay(g, r, c->d_b, p, s);
+  }
+  GBC_CUDA(cudaMemcpyAsync(c->h_cg, c->d_cg, sizeof(CGScalars) * n, cudaMemcpyDeviceToHost, s));
+  sync(c);
+  for (int i = 0; i < n; ++i) {
+    st.iters[i] = c->h_cg[i].iters;
+    if (c->h_cg[i].active && st.status[i] == GBC_OK) st.status[i] = GBC_ERR_NOT_CONVERGED;
+  }
+  return st;
+}
+
+// Chroma's RelInvCG_a, batched: b, psi in FP64; x, r in FP32; p, mp, mmp in the sloppy precision.
+CgStats reliable_cg(gbc_ctx* c, int po, const Spinor& psi, const Spinor& chi, double rsd, double delta, int maxit) {
+  const int n = psi.nrhs;
+  const Geom& g = c->g;
+  cudaStream_t s = c->stream;
+  const int D = PREC_DOUBLE, S = PREC_SINGLE;
+  Spinor b = sub(workspace(c, SLOT_BD, D, n), 0, n);
+  Spinor rd = sub(workspace(c, SLOT_RD, D, n), 0, n);
+  Spinor xd = sub(workspace(c, SLOT_XD, D, n), 0, n);
+  Spinor t1 = sub(workspace(c, SLOT_TD1, D, n), 0, n);
+  Spinor ted = sub(workspace(c, SLOT_TED, D, n), 0, n);
+  Spinor x = sub(workspace(c, SLOT_XS, S, n), 0, n);
+  Spinor r = sub(workspace(c, SLOT_RS, S, n), 0, n);
+  Spinor p = sub(workspace(c, SLOT_P + 100 * pidx(po), po, n), 0, n);
+  Spinor mp = sub(workspace(c, SLOT_MP + 100 * pidx(po), po, n), 0, n);
+  Spinor mmp = sub(workspace(c, SLOT_MMP + 100 * pidx(po), po, n), 0, n);
+  Spinor te = sub(workspace(c, SLOT_TE + 100 * pidx(po), po, n), 0, n);
+  CgStats st;
+  st.iters.assign(n, 0);
+  st.status.assign(n, GBC_OK);
+  std::vector<double> chi_norm = norm2(c, chi);
+  // b = chi - A psi
+  apply_sys(c, D, true, psi, b, t1, ted);
+  blas_xmy_norm2(g, chi, b, red(c), s);
+  std::vector<double> r_sq = fetch(c, 1, n);
+  blas_copy(g, r, b, s);
+  blas_zero(g, x, s);
+  std::vector<double> rNorm(n), r0Norm(n), maxrx(n), maxrr(n), cc(n, 0.0), rsd_sq(n);
+  std::vector<int> conv(n, 0);
+  for (int i = 0; i < n; ++i) {
+    rsd_sq[i] = rsd * rsd * chi_norm[i];
+    rNorm[i] = r0Norm[i] = maxrx[i] = maxrr[i] = std::sqrt(r_sq[i]);
+    if (r_sq[i] < rsd_sq[i]) conv[i] = 1;
+  }
+  std::vector<double> hb(n), ha(n);
+  int k;
+  auto all_conv = [&]() {
+    for (int i = 0; i < n; ++i)
+      if (!conv[i]) return false;
+    return true;
+  };
+  for (k = 0; k < maxit && !all_conv(); ++k) {
+    if (k == 0) {
+      blas_copy(g, p, r, s);
+    } else {
+      for (int i = 0; i < n; ++i) hb[i] = conv[i] ? 0.0 : r_sq[i] / cc[i];
+      GBC_CUDA(cudaMemcpyAsync(c->d_b, hb.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+      blas_xpay(g, r, c->d_b, p, s);
+    }
+    cc = r_sq;
+    apply_meo(c, po, false, p, mp, te, true);
+    std::vector<double> d = fetch(c, 1, n);
+    apply_meo(c, po, true, mp, mmp, te, false);
+    for (int i = 0; i < n; ++i) ha[i] = (conv[i] || !(d[i] > 0)) ? 0.0 : cc[i] / d[i];
+    GBC_CUDA(cudaMemcpyAsync(c->d_a, ha.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    blas_cg_update(g, c->d_a, x, p, r, mmp, red(c), s);
+    std::vector<double> nr = fetch(c, 1, n);
+    bool updR = false, updX = false;
+    for (int i = 0; i < n; ++i) {
+      if (conv[i]) continue;
+      ++st.iters[i];
+      r_sq[i] = nr[i];
+      if (!std::isfinite(nr[i])) {
+        st.status[i] = GBC_ERR_NONFINITE;
+        conv[i] = 1;
+        continue;
+      }
+      rNorm[i] = std::sqrt(r_sq[i]);
+      maxrx[i] = std::max(maxrx[i], rNorm[i]);
+      maxrr[i] = std::max(maxrr[i], rNorm[i]);
+      bool ux = rNorm[i] < delta * r0Norm[i] && r0Norm[i] <= maxrx[i];
+      bool ur = (rNorm[i] < delta * maxrr[i] && r0Norm[i] <= maxrr[i]) || ux;
+      updX |= ux;
+      updR |= ur;
+    }
+    if (updR) {
+      // r_dble = b - A (x promoted); r = r_dble (reliable_cg.cc:120-139)
+      blas_copy(g, xd, x, s);
+      apply_sys(c, D, true, xd, rd, t1, ted);
+      blas_xmy_norm2(g, b, rd, red(c), s);
+      std::vector<double> rr = fetch(c, 1, n);
+      blas_copy(g, r, rd, s);
+      ++st.reliable;
+      for (int i = 0; i < n; ++i) {
+        if (conv[i]) continue;
+        r_sq[i] = rr[i];
+        rNorm[i] = std::sqrt(rr[i]);
+        maxrr[i] = rNorm[i];
+      }
+      if (updX) {
+        // group-wise x update (reliable_cg.cc:141-151), for the whole batch
+        blas_xpy(g, psi, xd, s);
+        blas_zero(g, x, s);
+        blas_copy(g, b, rd, s);
+        for (int i = 0; i < n; ++i) {
+          if (conv[i]) continue;
+          r0Norm[i] = rNorm[i];
+          maxrx[i] = rNorm[i];
+        }
+      }
+    }
+    for (int i = 0; i < n; ++i)
+      if (!conv[i] && r_sq[i] < rsd_sq[i]) conv[i] = 1;
+  }
+  blas_xpy(g, psi, x, s);
+  for (int i = 0; i < n; ++i)
+    if (!conv[i] && st.status[i] == GBC_OK) st.status[i] = GBC_ERR_NOT_CONVERGED;
+  return st;
+}
+
+}  // namespace
+
+int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_canon, const double* chi_canon,
+                 gbc_result* res) {
+  gbc_solve_params p = *pp;
+  if (!(p.rsd_target > 0)) p.rsd_target = 1e-10;
+  if (p.max_iter <= 0) p.max_iter = 10000;
+  if (!(p.delta > 0)) p.delta = 0.1;
+  if (!(p.rsd_tolerance_factor > 0)) p.rsd_tolerance_factor = 10.0;
+  if (!(p.inner_tol > 0)) p.inner_tol = 1e-5;
+  if (p.inner_max_iter <= 0) p.inner_max_iter = p.max_iter;
+  if (p.nkrylov <= 0) p.nkrylov = 16;
+  int sloppy = p.sloppy_precision ? p.sloppy_precision : c->opts.sloppy_precision;
+  if (sloppy != PREC_HALF && sloppy != PREC_SINGLE && sloppy != PREC_DOUBLE) return GBC_ERR_ARGS;
+  if (p.system < GBC_SYS_MEO || p.system > GBC_SYS_FULL) return GBC_ERR_ARGS;
+  if (p.solver < GBC_SOLVER_CG || p.solver > GBC_SOLVER_FGMRES) return GBC_ERR_ARGS;
+
+  const int D = PREC_DOUBLE;
+  const Geom& g = c->g;
+  cudaStream_t s = c->stream;
+  const size_t rs = (size_t)c->V * 24;
+  ensure_prec(c, D);
+  if (p.solver != GBC_SOLVER_CG) {
+    ensure_prec(c, sloppy);
+    ensure_prec(c, PREC_SINGLE);
+  }
+  cudaEvent_t ev0, ev1;
+  GBC_CUDA(cudaEventCreate(&ev0));
+  GBC_CUDA(cudaEventCreate(&ev1));
+  GBC_CUDA(cudaEventRecord(ev0, s));
+  const int n = nrhs;
+  Spinor chi = sub(workspace(c, SLOT_B, D, n), 0, n);    // odd right-hand side of the odd system
+  Spinor psi = sub(workspace(c, SLOT_X, D, n), 0, n);    // odd solution
+  Spinor t1 = sub(workspace(c, SLOT_TD1, D, n), 0, n);
+  Spinor t2 = sub(workspace(c, SLOT_TD2, D, n), 0, n);
+  Spinor ted = sub(workspace(c, SLOT_TED, D, n), 0, n);
+  const PrecFields& fd = c->pf[pidx(D)];
+
+  import_spinor(g, chi_canon, rs, 1, chi, s);
+  Spinor chie, psie;
+  if (p.system == GBC_SYS_FULL) {
+    // Schur prep (eoprec_fermact_qprop.cc:47-54): chi'_o = chi_o - (-1/2 D_oe) A_ee^-1 chi_e
+    chie = sub(workspace(c, SLOT_CHIE, D, n), 0, n);
+    psie = sub(workspace(c, SLOT_PSIE, D, n), 0, n);
+    import_spinor(g, chi_canon, rs, 0, chie, s);
+    apply_clover(c, D, 0, true, chie, ted);
+    hop(c, D, 1, HOP_PLAIN, false, 0.5, ted, t1, nullptr, nullptr, false);
+    blas_xpy(g, chi, t1, s);
+  }
+  if (p.zero_guess) blas_zero(g, psi, s);
+  else import_spinor(g, psi_canon, rs, 1, psi, s);
+
+  const bool mdagm = p.system == GBC_SYS_MDAGM;
+  std::vector<int> iters(n, 0), status(n, GBC_OK), outer(n, 0);
+  int reliable = 0;
+
+  if (p.solver == GBC_SOLVER_CG) {
+    // chi' = M~^dag chi (LinOp) ; InvCG2 on M~^dag M~
+    Spinor rhs = chi;
+    if (!mdagm) {
+      rhs = sub(workspace(c, SLOT_RHS, D, n), 0, n);
+      apply_meo(c, D, true, chi, rhs, ted, false);
+    }
+    CgCfg cfg{D, D, p.rsd_target, p.max_iter, 0.0, 4};
+    CgStats st = cg_normal(c, cfg, psi, rhs, p.zero_guess != 0, std::vector<int>(n, 1));
+    iters = st.iters;
+    status = st.status;
+  } else if (p.solver == GBC_SOLVER_RELIABLE_CG) {
+    Spinor rhs = chi;
+    if (!mdagm) {
+      rhs = sub(workspace(c, SLOT_RHS, D, n), 0, n);
+      apply_meo(c, D, true, chi, rhs, ted, false);
+    }
+    int po = sloppy == PREC_DOUBLE ? PREC_SINGLE : sloppy;
+    CgStats st = reliable_cg(c, po, psi, rhs, p.rsd_target, p.delta, p.max_iter);
+    iters = st.iters;
+    status = st.status;
+    reliable = st.reliable;
+  } else if (p.solver == GBC_SOLVER_MIXED || p.solver == GBC_SOLVER_FGMRES) {
+    // FP64 defect correction: r = chi - A psi; solve A e = r in low precision; psi += e
+    const int S = PREC_SINGLE;
+    const int pa = sloppy == PREC_DOUBLE ? D : S;
+    Spinor rd = sub(workspace(c, SLOT_RD, D, n), 0, n);
+    Spinor rsl = sub(workspace(c, SLOT_RS, pa, n), 0, n);
+    Spinor es = sub(workspace(c, SLOT_ES, pa, n), 0, n);
+    Spinor rhs = sub(workspace(c, SLOT_SE, pa, n), 0, n);
+    Spinor teh = sub(workspace(c, SLOT_TEH + 50, pa, n), 0, n);
+    std::vector<double> bb = norm2(c, chi);
+    std::vector<int> done(n, 0);
+    for (int i = 0; i < n; ++i)
+      if (!std::isfinite(bb[i])) {
+        status[i] = GBC_ERR_NONFINITE;
+        done[i] = 1;
+      }
+    const int max_outer = 50;
+    int total = 0;
+    for (int it = 0; it <= max_outer; ++it) {
+      // FP64 residual
+      if (it == 0 && p.zero_guess) {
+        blas_copy(g, rd, chi, s);
+        blas_norm2(g, rd, red(c), s);
+      } else {
+        apply_sys(c, D, mdagm, psi, rd, t2, ted);
+        blas_xmy_norm2(g, chi, rd, red(c), s);
+      }
+      std::vector<double> rr = fetch(c, 1, n);
+      bool all = true;
+      for (int i = 0; i < n; ++i) {
+        if (done[i]) continue;
+        if (!std::isfinite(rr[i])) {
+          status[i] = GBC_ERR_NONFINITE;
+          done[i] = 1;
+          continue;
+        }
+        if (rr[i] <= p.rsd_target * p.rsd_target * bb[i]) done[i] = 1;
+        else all = false;
+      }
+      if (all || it == max_outer || total >= p.max_iter) break;
+      std::vector<int> active(n);
+      for (int i = 0; i < n; ++i) {
+        active[i] = !done[i];
+        if (active[i]) ++outer[i];
+      }
+      // inner right-hand side in the accumulator precision
+      blas_copy(g, rsl, rd, s);
+      if (!mdagm) apply_meo(c, pa, true, rsl, rhs, teh, false);
+      else blas_copy(g, rhs, rsl, s);
+      // never ask the inner solve for more than the outer target needs
+      CgCfg cfg{pa, sloppy, p.inner_tol, p.inner_max_iter, p.delta, 1};
+      CgStats st = cg_normal(c, cfg, es, rhs, true, active);
+      reliable += st.reliable;
+      int mx = 0;
+      for (int i = 0; i < n; ++i) {
+        iters[i] += st.iters[i];
+        mx = std::max(mx, st.iters[i]);
+        if (st.status[i] == GBC_ERR_NONFINITE) {
+          status[i] = GBC_ERR_NONFINITE;
+          done[i] = 1;
+        }
+      }
+      total += mx;
+      blas_xpy(g, psi, es, s);
+    }
+    for (int i = 0; i < n; ++i)
+      if (!done[i] && status[i] == GBC_OK) status[i] = GBC_ERR_NOT_CONVERGED;
+  }
+
+  // true FP64 residual of the system solved, then even reconstruction for the full system
+  std::vector<double> bb = norm2(c, chi);
+  apply_sys(c, D, mdagm, psi, t1, t2, ted);
+  blas_xmy_norm2(g, chi, t1, red(c), s);
+  std::vector<double> rr = fetch(c, 1, n);
+  export_spinor(g, psi_canon, rs, 1, psi, s);
+  if (p.system == GBC_SYS_FULL) {
+    // psi_e = A_ee^-1 (chi_e + 1/2 D_eo psi_o)   (eoprec_fermact_qprop.cc:60-67)
+    hop(c, D, 0, HOP_PLAIN, false, 0.5, psi, t1, nullptr, nullptr, false);
+    blas_xpy(g, t1, chie, s);
+    apply_clover(c, D, 0, true, t1, psie);
+    export_spinor(g, psi_canon, rs, 0, psie, s);
+    // full residual |M psi - chi| over both parities (eoprec_fermact_qprop.cc:70-76)
+    Spinor ue = sub(workspace(c, SLOT_T1, D, n), 0, n);
+    Spinor uo = sub(workspace(c, SLOT_T2, D, n), 0, n);
+    hop(c, D, 0, HOP_XPAY, false, -0.5, psi, ue, &psie, fd.clov[0], false);
+    hop(c, D, 1, HOP_XPAY, false, -0.5, psie, uo, &psi, fd.clov[1], false);
+    Spinor chio = sub(workspace(c, SLOT_PSIE + 50, D, n), 0, n);
+    import_spinor(g, chi_canon, rs, 1, chio, s);
+    blas_xmy_norm2(g, chie, ue, red(c), s);
+    std::vector<double> re = fetch(c, 1, n);
+    blas_xmy_norm2(g, chio, uo, red(c), s);
+    std::vector<double> ro = fetch(c, 1, n);
+    std::vector<double> ne = norm2(c, chie), no = norm2(c, chio);
+    for (int i = 0; i < n; ++i) {
+      rr[i] = re[i] + ro[i];
+      bb[i] = ne[i] + no[i];
+    }
+  }
+  GBC_CUDA(cudaGetLastError());
+  GBC_CUDA(cudaEventRecord(ev1, s));
+  GBC_CUDA(cudaEventSynchronize(ev1));
+  float ms = 0;
+  GBC_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  int worst = GBC_OK;
+  for (int i = 0; i < n; ++i) {
+    gbc_result& o = res[i];
+    std::memset(&o, 0, sizeof(o));
+    o.device_seconds = ms * 1e-3;
+    o.n_count = iters[i];
+    o.resid = std::sqrt(rr[i]);
+    o.rel_resid = bb[i] > 0 ? std::sqrt(rr[i] / bb[i]) : o.resid;
+    o.n_outer = outer[i];
+    o.n_reliable = reliable;
+    o.status = status[i];
+    if (!std::isfinite(o.resid)) o.status = GBC_ERR_NONFINITE;
+    // RsdToleranceFactor check (syssolver_linop_clover_quda_w.h:636-643)
+    if (o.status == GBC_ERR_NOT_CONVERGED && o.rel_resid <= p.rsd_tolerance_factor * p.rsd_target) o.status = GBC_OK;
+    if (o.status == GBC_OK && !(o.rel_resid <= p.rsd_tolerance_factor * p.rsd_target)) o.status = GBC_ERR_NOT_CONVERGED;
+    if (o.status != GBC_OK && worst == GBC_OK) worst = o.status;
+  }
+  return worst;
+}
+
+}  // namespace gbc

@@ -1,0 +1,224 @@
+"""ctypes binding of ``libgbclover.so`` (include/gbclover.h).
+
+Plain host arrays only: complex128 numpy arrays in the canonical layouts of the header
+(links (V, 4, 3, 3), spinors (nrhs, V, 4, 3) or (V, 4, 3)).  Device pointers (for the
+resident-input path) are passed as integers.  There is no CPU fallback: if the library
+cannot be loaded, or no CUDA device is present, the calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libgbclover.so")
+
+GBC_OK = 0
+ERRORS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "solver did not converge", 4: "Krylov breakdown",
+          5: "non-finite value", 6: "invalid call order", 7: "12-real reconstruction not possible",
+          8: "learned preconditioner unavailable"}
+PREC_HALF, PREC_SINGLE, PREC_DOUBLE = 2, 4, 8
+RECON_18, RECON_12 = 18, 12
+OP_DSLASH, OP_CLOVER, OP_CLOVINV, OP_MEO, OP_MDAGM, OP_UNPREC = range(6)
+SOLVER_CG, SOLVER_RELIABLE_CG, SOLVER_MIXED, SOLVER_FGMRES = range(4)
+SYS_MEO, SYS_MDAGM, SYS_FULL = range(3)
+
+# every entry point include/gbclover.h declares
+EXPORTS = ["gbc_create", "gbc_destroy", "gbc_strerror", "gbc_last_error", "gbc_load_gauge", "gbc_load_clover",
+           "gbc_get_clover", "gbc_apply", "gbc_solve", "gbc_solve_device", "gbc_load_precond",
+           "gbc_gauge_synthetic", "gbc_time_operator"]
+
+
+class Geom(C.Structure):
+    _fields_ = [("dims", C.c_int * 4), ("t_boundary", C.c_int)]
+
+
+class Action(C.Structure):
+    _fields_ = [("mass", C.c_double), ("clov_coeff_r", C.c_double), ("clov_coeff_t", C.c_double),
+                ("aniso", C.c_int), ("xi_0", C.c_double), ("nu", C.c_double), ("t_dir", C.c_int),
+                ("twisted", C.c_int), ("twisted_m", C.c_double)]
+
+
+class Opts(C.Structure):
+    _fields_ = [("sloppy_precision", C.c_int), ("sloppy_reconstruct", C.c_int), ("max_rhs", C.c_int),
+                ("verbose", C.c_int)]
+
+
+class SolveParams(C.Structure):
+    _fields_ = [("solver", C.c_int), ("system", C.c_int), ("rsd_target", C.c_double), ("max_iter", C.c_int),
+                ("delta", C.c_double), ("rsd_tolerance_factor", C.c_double), ("sloppy_precision", C.c_int),
+                ("inner_tol", C.c_double), ("inner_max_iter", C.c_int), ("nkrylov", C.c_int),
+                ("use_precond", C.c_int), ("zero_guess", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("n_count", C.c_int), ("status", C.c_int), ("resid", C.c_double), ("rel_resid", C.c_double),
+                ("seconds", C.c_double), ("n_outer", C.c_int), ("n_reliable", C.c_int),
+                ("device_seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the CUDA library (raises if it was not built: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} missing: run __graft_entry__.build() (nvcc, sm_103a) first")
+    lib = C.CDLL(path)
+    dp = C.POINTER(C.c_double)
+    lib.gbc_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(Geom), C.POINTER(Action), C.POINTER(Opts)]
+    lib.gbc_destroy.argtypes = [C.c_void_p]
+    lib.gbc_destroy.restype = None
+    lib.gbc_strerror.restype = C.c_char_p
+    lib.gbc_strerror.argtypes = [C.c_int]
+    lib.gbc_last_error.restype = C.c_char_p
+    lib.gbc_last_error.argtypes = [C.c_void_p]
+    lib.gbc_load_gauge.argtypes = [C.c_void_p, dp]
+    lib.gbc_load_clover.argtypes = [C.c_void_p, dp, dp]
+    lib.gbc_get_clover.argtypes = [C.c_void_p, dp, dp, dp, C.POINTER(C.c_int)]
+    lib.gbc_apply.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp]
+    lib.gbc_solve.argtypes = [C.c_void_p, C.POINTER(SolveParams), C.c_int, dp, dp, C.POINTER(Result)]
+    lib.gbc_solve_device.argtypes = [C.c_void_p, C.POINTER(SolveParams), C.c_int, C.c_void_p, C.c_void_p,
+                                     C.POINTER(Result)]
+    lib.gbc_load_precond.argtypes = [C.c_void_p, C.c_char_p]
+    lib.gbc_time_operator.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp]
+    lib.gbc_gauge_synthetic.argtypes = [C.POINTER(C.c_int), C.c_double, C.c_ulonglong, C.c_int, C.c_double,
+                                        C.POINTER(C.c_int), C.c_int, dp]
+    _lib = lib
+    return lib
+
+
+class GBCError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _dp(a):
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def gauge_synthetic(dims, eps, seed, n_stout=0, rho=0.0, smear_dirs=(1, 1, 1, 1), t_boundary=-1):
+    """Seeded hot-start links (host generator of the library), shape (V, 4, 3, 3) complex128."""
+    lib = load()
+    V = int(np.prod(dims))
+    u = np.empty((V, 4, 3, 3), dtype=np.complex128)
+    d = (C.c_int * 4)(*dims)
+    sd = (C.c_int * 4)(*smear_dirs)
+    rc = lib.gbc_gauge_synthetic(d, float(eps), int(seed), int(n_stout), float(rho), sd, int(t_boundary),
+                                 _dp(u.view(np.float64)))
+    if rc != GBC_OK:
+        raise GBCError(rc, "gauge_synthetic")
+    return u
+
+
+class Context:
+    """One solver context: links, clover term and workspaces on the GPU (one CUDA stream)."""
+
+    def __init__(self, dims, mass, clov_coeff, clov_coeff_t=None, t_boundary=-1, sloppy_precision=PREC_HALF,
+                 sloppy_reconstruct=RECON_12, max_rhs=12, aniso=None, twisted_m=None, verbose=False):
+        self.lib = load()
+        self.dims = tuple(int(d) for d in dims)
+        self.V = int(np.prod(self.dims))
+        g = Geom((C.c_int * 4)(*self.dims), int(t_boundary))
+        a = Action(float(mass), float(clov_coeff), float(clov_coeff if clov_coeff_t is None else clov_coeff_t),
+                   0, 1.0, 1.0, 3, int(twisted_m is not None), float(twisted_m or 0.0))
+        if aniso is not None:
+            a.aniso, a.xi_0, a.nu, a.t_dir = 1, float(aniso["xi_0"]), float(aniso["nu"]), int(aniso.get("t_dir", 3))
+        o = Opts(int(sloppy_precision), int(sloppy_reconstruct), int(max_rhs), int(bool(verbose)))
+        h = C.c_void_p()
+        rc = self.lib.gbc_create(C.byref(h), C.byref(g), C.byref(a), C.byref(o))
+        if rc != GBC_OK:
+            raise GBCError(rc, "gbc_create")
+        self.h = h
+        self.max_rhs = max_rhs
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != GBC_OK:
+            raise GBCError(rc, f"{what}: {self.lib.gbc_last_error(self.h).decode()}")
+
+    def load_gauge(self, links):
+        u = np.ascontiguousarray(links, dtype=np.complex128).reshape(self.V, 4, 3, 3)
+        self._check(self.lib.gbc_load_gauge(self.h, _dp(u.view(np.float64))), "load_gauge")
+
+    def load_clover(self, clov, invclov):
+        a = np.ascontiguousarray(clov, dtype=np.float64)
+        b = np.ascontiguousarray(invclov, dtype=np.float64)
+        self._check(self.lib.gbc_load_clover(self.h, _dp(a), _dp(b)), "load_clover")
+
+    def get_clover(self):
+        a = np.zeros((self.V, 72))
+        b = np.zeros((self.V, 72))
+        ld = C.c_double()
+        nn = C.c_int()
+        self._check(self.lib.gbc_get_clover(self.h, _dp(a), _dp(b), C.byref(ld), C.byref(nn)), "get_clover")
+        return a, b, ld.value, nn.value
+
+    def _fields(self, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        if x.size % (self.V * 12):
+            raise ValueError("spinor size")
+        return x.reshape(-1, self.V, 12)
+
+    def apply(self, op, x, isign=+1, cb=1, prec=PREC_DOUBLE, out=None):
+        x = self._fields(x)
+        nrhs = x.shape[0]
+        out = np.zeros_like(x) if out is None else self._fields(out).copy()
+        self._check(self.lib.gbc_apply(self.h, int(op), int(isign), int(cb), int(prec), nrhs,
+                                       _dp(out.view(np.float64)), _dp(x.view(np.float64))), "apply")
+        return out
+
+    def solve(self, chi, solver=SOLVER_CG, system=SYS_MEO, rsd_target=1e-10, max_iter=10000, delta=0.1,
+              sloppy_precision=0, inner_tol=0.0, nkrylov=16, use_precond=0, psi0=None, tol_factor=10.0,
+              raise_on_error=True):
+        chi = self._fields(chi)
+        nrhs = chi.shape[0]
+        psi = np.zeros_like(chi) if psi0 is None else self._fields(psi0).copy()
+        p = SolveParams(int(solver), int(system), float(rsd_target), int(max_iter), float(delta), float(tol_factor),
+                        int(sloppy_precision), float(inner_tol), 0, int(nkrylov), int(use_precond),
+                        int(psi0 is None))
+        res = (Result * nrhs)()
+        rc = self.lib.gbc_solve(self.h, C.byref(p), nrhs, _dp(psi.view(np.float64)), _dp(chi.view(np.float64)), res)
+        if rc != GBC_OK and raise_on_error:
+            self._check(rc, "solve")
+        return psi, [r.as_dict() for r in res], rc
+
+    def solve_device(self, psi_ptr, chi_ptr, nrhs, solver=SOLVER_CG, system=SYS_MEO, rsd_target=1e-10,
+                     max_iter=10000, delta=0.1, sloppy_precision=0, inner_tol=0.0, nkrylov=16, use_precond=0,
+                     zero_guess=True, tol_factor=10.0):
+        p = SolveParams(int(solver), int(system), float(rsd_target), int(max_iter), float(delta), float(tol_factor),
+                        int(sloppy_precision), float(inner_tol), 0, int(nkrylov), int(use_precond),
+                        int(bool(zero_guess)))
+        res = (Result * nrhs)()
+        rc = self.lib.gbc_solve_device(self.h, C.byref(p), int(nrhs), C.c_void_p(psi_ptr), C.c_void_p(chi_ptr), res)
+        return [r.as_dict() for r in res], rc
+
+    def time_operator(self, op, prec, nrhs=1, iters=20, flush_l2=True):
+        """Mean seconds per application and algorithmic bytes (CUDA events on the context stream)."""
+        sec = C.c_double()
+        byt = C.c_double()
+        self._check(self.lib.gbc_time_operator(self.h, int(op), int(prec), int(nrhs), int(iters), int(bool(flush_l2)),
+                                               C.byref(sec), C.byref(byt)), "time_operator")
+        return sec.value, byt.value
+
+    def load_precond(self, path):
+        self._check(self.lib.gbc_load_precond(self.h, path.encode()), "load_precond")

@@ -1,0 +1,190 @@
+/*
+ * gbclover.h -- C ABI of the GB300-native even-odd Wilson-clover solver.
+ *
+ * The library replaces the hot path of Chroma's propagator and HMC solves: the even-odd
+ * preconditioned clover operator (Chroma lib/actions/ferm/linop/eoprec_clover_linop_w.cc) and
+ * the solvers registered in TheLinOpFermSystemSolverFactory / TheMdagMFermSystemSolverFactory
+ * (lib/actions/ferm/invert/syssolver_linop_factory.h:29-39, syssolver_mdagm_factory.h:28-39).
+ * A Chroma-side adapter (chroma_plugin/) gathers QDP++ fields by lattice coordinate into the
+ * host layouts below and calls these entry points; the context owns every device allocation.
+ *
+ * Host layouts (all complex numbers are interleaved re, im doubles):
+ *   site index   s = x + Lx*(y + Ly*(z + Lz*t))                  (x fastest; NERSC order)
+ *   gauge links  double[V][4][3][3][2]   u[s][mu][row][col]      BC already applied
+ *   spinor       double[V][4][3][2]      psi[s][spin][colour]    DeGrand-Rossi gamma basis
+ *   clover       double[V][72]           Chroma's PrimitiveClovTriang per site
+ *                                        {diag[2][6], offd[2][15] complex}
+ *   nrhs fields are stored back to back (rhs stride = V*24 doubles).
+ * Parity of a site = (x+y+z+t) mod 2; parity 0 = Chroma's rb[0] (even), 1 = rb[1] (odd).
+ *
+ * Threading: one context = one CUDA stream; calls on one context must not overlap; separate
+ * contexts are independent.  Every call returns a status (GBC_OK = 0).
+ */
+#ifndef GBCLOVER_H
+#define GBCLOVER_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (gbc_strerror) --------------------------------------------------------- */
+#define GBC_OK 0
+#define GBC_ERR_ARGS 1          /* invalid argument / unsupported geometry */
+#define GBC_ERR_CUDA 2          /* CUDA runtime error (message in gbc_last_error) */
+#define GBC_ERR_NOT_CONVERGED 3 /* MaxIter reached above RsdToleranceFactor*RsdTarget */
+#define GBC_ERR_BREAKDOWN 4     /* Krylov breakdown */
+#define GBC_ERR_NONFINITE 5     /* NaN/Inf in a source, field or residual */
+#define GBC_ERR_STATE 6         /* call order (e.g. solve before gauge load) */
+#define GBC_ERR_RECON 7         /* 12-real reconstruction requested for non-SU(3) links */
+#define GBC_ERR_PRECOND 8       /* learned preconditioner weights missing or corrupt */
+
+/* ---- enums ------------------------------------------------------------------------------- */
+/* precisions: QUDA_..._PRECISION of syssolver_quda_clover_params.cc (HALF/SINGLE/DOUBLE) */
+#define GBC_PREC_HALF 2
+#define GBC_PREC_SINGLE 4
+#define GBC_PREC_DOUBLE 8
+/* gauge reconstruction: RECONS_NONE = 18 reals, RECONS_12 */
+#define GBC_RECON_18 18
+#define GBC_RECON_12 12
+/* operators for gbc_apply (parity tests; mirror the EvenOddPrecLinearOperator blocks) */
+#define GBC_OP_DSLASH 0   /* D' on output parity cb (lwldslash_w.h:226-303)                         */
+#define GBC_OP_CLOVER 1   /* A on parity cb (clover_term_qdp_w.h:2138-2160)                         */
+#define GBC_OP_CLOVINV 2  /* A^-1 on the even parity (invclov, eoprec_clover_linop_w.cc:75-86)       */
+#define GBC_OP_MEO 3      /* M~ = A_oo - 1/4 D_oe A_ee^-1 D_eo on odd sites (eoprec_clover_linop_w.cc:142-187) */
+#define GBC_OP_MDAGM 4    /* M~^dag M~ (lib/lmdagm.h)                                                */
+#define GBC_OP_UNPREC 5   /* full unpreconditioned M (lib/eoprec_linop.h:147-165)                    */
+/* solvers (Chroma invType they stand in for) */
+#define GBC_SOLVER_CG 0           /* CG_INVERTER: CGNE, InvCG2 (invcg2.cc:70-232), FP64           */
+#define GBC_SOLVER_RELIABLE_CG 1  /* RELIABLE_CG_MP_CLOVER_INVERTER (reliable_cg.cc:10-188)         */
+#define GBC_SOLVER_MIXED 2        /* RICHARDSON_MP_CLOVER_INVERTER pattern: FP64 defect correction
+                                     around a reliable-update CGNE in sloppy precision
+                                     (inv_multiprec_richardson.cc:13-107)                            */
+#define GBC_SOLVER_FGMRES 3       /* FGMRESDR_INVERTER with NDefl = 0 (syssolver_linop_fgmres_dr.cc),
+                                     preconditioned by the learned network when loaded               */
+/* linear systems */
+#define GBC_SYS_MEO 0    /* M~ psi_o = chi_o           (LinOpSystemSolver, syssolver_linop.h)          */
+#define GBC_SYS_MDAGM 1  /* M~^dag M~ psi_o = chi_o    (MdagMSystemSolver, syssolver_mdagm.h:25-35)    */
+#define GBC_SYS_FULL 2   /* M psi = chi on both parities: Schur prep, odd solve, even reconstruction
+                            (PrecFermActQprop, eoprec_fermact_qprop.cc:41-80)                        */
+
+/* ---- parameter structs ------------------------------------------------------------------- */
+typedef struct gbc_geom {
+  int dims[4];    /* Lx, Ly, Lz, Lt; Lx even, every extent >= 2 */
+  int t_boundary; /* +1 periodic, -1 antiperiodic in time: the sign already folded into the links
+                     at t = Lt-1 (SimpleFermBC::modify, simple_fermbc.h:87-104); used by the
+                     12-real reconstruction */
+} gbc_geom;
+
+/* CloverFermActParams (clover_fermact_params_w.cc:27-99) */
+typedef struct gbc_action {
+  double mass;          /* Mass = 1/(2 Kappa) - 4  (param_io.cc:12-15)            */
+  double clov_coeff_r;  /* clovCoeffR (= clovCoeff when isotropic)                */
+  double clov_coeff_t;  /* clovCoeffT                                             */
+  int aniso;            /* AnisoParam.anisoP                                       */
+  double xi_0, nu;      /* AnisoParam.xi_0, AnisoParam.nu                          */
+  int t_dir;            /* AnisoParam.t_dir (3)                                    */
+  int twisted;          /* TwistedM present                                       */
+  double twisted_m;     /* TwistedM                                               */
+} gbc_action;
+
+typedef struct gbc_opts {
+  int sloppy_precision;   /* CudaSloppyPrecision: GBC_PREC_HALF / SINGLE / DOUBLE  */
+  int sloppy_reconstruct; /* CudaSloppyReconstruct: GBC_RECON_12 / GBC_RECON_18    */
+  int max_rhs;            /* largest nrhs a solve will be given (workspace sizing) */
+  int verbose;
+} gbc_opts;
+
+/* per-call solve parameters (SysSolverQUDACloverParams fields, syssolver_quda_clover_params.h:15-90) */
+typedef struct gbc_solve_params {
+  int solver;                 /* GBC_SOLVER_*                                       */
+  int system;                 /* GBC_SYS_*                                          */
+  double rsd_target;          /* RsdTarget: relative residual |chi - A psi| / |chi| */
+  int max_iter;               /* MaxIter                                            */
+  double delta;               /* Delta (reliable-update trigger)                    */
+  double rsd_tolerance_factor;/* RsdToleranceFactor: failure threshold (default 10)  */
+  int sloppy_precision;       /* 0 = context default                                */
+  double inner_tol;           /* GBC_SOLVER_MIXED inner relative tolerance (0 = 1e-5)*/
+  int inner_max_iter;         /* 0 = max_iter                                       */
+  int nkrylov;                /* FGMRES NKrylov (0 = 16)                            */
+  int use_precond;            /* FGMRES: apply the loaded learned preconditioner     */
+  int zero_guess;             /* 1: ignore psi on entry (qprop passes zero)          */
+} gbc_solve_params;
+
+/* SystemSolverResults_t (lib/syssolver.h:16-23) plus what the adapter logs */
+typedef struct gbc_result {
+  int n_count;        /* iterations (operator applications / 2 for CGNE)      */
+  int status;         /* GBC_OK or an error code for this right-hand side     */
+  double resid;       /* |chi - A psi| on the system's sites, FP64             */
+  double rel_resid;   /* resid / |chi|                                         */
+  double seconds;     /* wall time of the whole call                           */
+  int n_outer;        /* outer (FP64) iterations of the mixed solvers          */
+  int n_reliable;     /* reliable updates                                      */
+  double device_seconds; /* CUDA-event time of the solve on the context stream  */
+} gbc_result;
+
+typedef struct gbc_ctx gbc_ctx;
+
+/* ---- lifecycle -------------------------------------------------------------------------- */
+/* Replaces the constructor of the solver adapter (cf. LinOpSysSolverQUDAClover ctor,
+   syssolver_linop_clover_quda_w.h:50-566).  opts may be NULL (defaults: HALF, RECON_12, 12). */
+int gbc_create(gbc_ctx** ctx, const gbc_geom* geom, const gbc_action* act, const gbc_opts* opts);
+/* Replaces ~LinOpSysSolverQUDAClover (syssolver_linop_clover_quda_w.h:570-575). */
+void gbc_destroy(gbc_ctx* ctx);
+const char* gbc_strerror(int status);
+const char* gbc_last_error(gbc_ctx* ctx);
+
+/* ---- fields ------------------------------------------------------------------------------ */
+/* Links from FermState::getLinks() (BC applied, possibly smeared); builds the clover term and
+   its even-parity inverse on the device (QDPCloverTermT::create + choles(0),
+   clover_term_qdp_w.h:244-294, 560-571; cf. loadGaugeQuda/loadCloverQuda of
+   syssolver_linop_clover_quda_w.h:523,552). */
+int gbc_load_gauge(gbc_ctx* ctx, const double* links);
+/* Optional: replace the clover term with host-packed A (all sites) and A^-1 (even sites),
+   e.g. from QDPCloverTermT::packForQUDA's source (clover_term_qdp_w.h:2221-2228). */
+int gbc_load_clover(gbc_ctx* ctx, const double* clov, const double* invclov_even);
+/* Packed A and A^-1 (even sites; odd sites zero) and sum_even log|d| (cholesDet(0),
+   clover_term_qdp_w.h:580-606); any output pointer may be NULL. */
+int gbc_get_clover(gbc_ctx* ctx, double* clov, double* invclov, double* logdet_even, int* n_negative);
+
+/* ---- operators (parity tests; LinearOperator<LatticeFermion>::operator(), lib/linearop.h:25-49) */
+/* out/in: nrhs host spinors (full lattice); only the parity the operator reads/writes matters;
+   sites of the other parity in out are left untouched.  prec selects the storage precision
+   the operator runs in (GBC_PREC_DOUBLE for the FP64 path). */
+int gbc_apply(gbc_ctx* ctx, int op, int isign, int cb, int prec, int nrhs, double* out, const double* in);
+
+/* ---- solves (LinOpSystemSolver::operator()(psi, chi), lib/syssolver.h:32-50) --------------- */
+/* psi, chi: nrhs host spinors, full lattice.  GBC_SYS_MEO / MDAGM read chi and psi on the odd
+   sites and write psi there; GBC_SYS_FULL reads chi everywhere and writes psi everywhere.
+   res: nrhs results.  Returns the worst status over the right-hand sides. */
+int gbc_solve(gbc_ctx* ctx, const gbc_solve_params* p, int nrhs, double* psi, const double* chi, gbc_result* res);
+/* Same with psi and chi already in device memory (same canonical layout). */
+int gbc_solve_device(gbc_ctx* ctx, const gbc_solve_params* p, int nrhs, double* psi_dev, const double* chi_dev,
+                     gbc_result* res);
+
+/* ---- measurement (the timing loops of Chroma's t_clover.cc:16-212 / t_lwldslash_sse.cc:20-215) */
+/* Times `iters` applications of op (GBC_OP_DSLASH: one hopping launch; GBC_OP_MEO: the two fused
+   launches of M~) on device-resident pseudo-random fields of nrhs right-hand sides in precision
+   prec, with CUDA events on the context stream.  flush_l2 != 0 overwrites a 256 MiB buffer
+   between launches, outside the timed events.  seconds = mean per application; bytes = the
+   compulsory (algorithmic) DRAM bytes of one application:
+     D'  : Vh (8 L + 2 n S)        M~ : Vh (16 L + 2 C + 5 n S)
+   with L, S, C the stored bytes of a link, a spinor (+ its norm in half) and a clover site. */
+int gbc_time_operator(gbc_ctx* ctx, int op, int prec, int nrhs, int iters, int flush_l2, double* seconds,
+                      double* bytes);
+
+/* ---- learned preconditioner --------------------------------------------------------------- */
+/* Load network weights (versioned binary, see gbc_precond_save) for use inside FGMRES. */
+int gbc_load_precond(gbc_ctx* ctx, const char* path);
+
+/* ---- synthetic inputs ---------------------------------------------------------------------- */
+/* Seeded hot-start links U = reunit(exp(i eps H)), H traceless Hermitian with Gaussian entries,
+   then n_stout stout steps of size rho in the directions with smear_dirs[mu] != 0
+   (stout_utils.cc:105-180, 936-966), then the time boundary sign t_boundary at t = Lt-1.
+   Host code (OpenMP); the counter-based recipe is given in the implementation. */
+int gbc_gauge_synthetic(const int dims[4], double eps, unsigned long long seed, int n_stout, double rho,
+                        const int smear_dirs[4], int t_boundary, double* links);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBCLOVER_H */

@@ -1,0 +1,148 @@
+"""GPU parity of the sm_103a kernels against the CPU oracle, through the C ABI.
+
+Tolerances (relative, |gpu - oracle| / |oracle| over the whole output field):
+  FP64 storage and arithmetic      1e-12
+  FP32 storage and arithmetic      1e-6
+  FP16 storage, FP32 arithmetic    5e-3
+Solvers: the FP64 true relative residual |chi - A psi| / |chi| computed by the oracle operator is
+<= 1e-10 (the target), and the error against the oracle's own FP64 solution is reported.
+"""
+import numpy as np
+import pytest
+
+from chroma_gb300 import gbclover as G
+from chroma_gb300 import sources as S
+
+pytestmark = pytest.mark.gpu
+
+KAPPA = 0.115
+CSW = 1.0
+TOL = {G.PREC_DOUBLE: 1e-12, G.PREC_SINGLE: 1e-6, G.PREC_HALF: 5e-3}
+
+
+def rel(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+@pytest.fixture(scope="module", params=[(4, 4, 4, 8), (8, 8, 8, 8)], ids=["4x4x4x8", "8^4"])
+def setup(request):
+    from oracle import Oracle, OracleOp
+    dims = request.param
+    o = Oracle()
+    u = o.apply_bc(dims, o.gauge_hot(dims, 0.3, 1234), (1, 1, 1, -1))
+    mass = 1 / (2 * KAPPA) - 4
+    op = OracleOp(dims, u, mass, CSW)
+    ctx = G.Context(dims, mass, CSW, t_boundary=-1, max_rhs=12)
+    ctx.load_gauge(u)
+    yield dims, op, ctx
+    ctx.close()
+
+
+def test_clover_build_matches(setup):
+    dims, op, ctx = setup
+    c, ci, ld, nn = ctx.get_clover()
+    oc, oci = op.clover()
+    assert rel(c, oc) < 1e-13
+    par = S.parity(dims)
+    assert rel(ci[par == 0], oci[par == 0]) < 1e-12
+    assert abs(ld - op.logdet_even()) < 1e-10 * abs(op.logdet_even())
+    assert nn == op.neg_eigs()
+
+
+@pytest.mark.parametrize("prec", [G.PREC_DOUBLE, G.PREC_SINGLE, G.PREC_HALF], ids=["f64", "f32", "f16"])
+@pytest.mark.parametrize("isign", [1, -1])
+def test_operators(setup, prec, isign):
+    from oracle import oracle as O
+    dims, op, ctx = setup
+    V = int(np.prod(dims))
+    x = S.gaussian(dims, 7).reshape(V, 12)
+    cases = [(G.OP_DSLASH, O.OP_DSLASH, 0), (G.OP_DSLASH, O.OP_DSLASH, 1), (G.OP_CLOVER, O.OP_CLOVER, 1),
+             (G.OP_CLOVER, O.OP_CLOVER, 0), (G.OP_CLOVINV, O.OP_CLOVER_INV, 0), (G.OP_MEO, O.OP_MEO, 1),
+             (G.OP_UNPREC, O.OP_UNPREC, 0)]
+    if isign == 1:
+        cases.append((G.OP_MDAGM, O.OP_MDAGM, 1))
+    par = S.parity(dims)
+    for gop, oop, cb in cases:
+        want = op.apply(oop, x, isign, cb)
+        got = ctx.apply(gop, x, isign, cb, prec)[0]
+        if gop == G.OP_UNPREC:
+            err = rel(got, want)
+        else:
+            err = rel(got[par == cb], want[par == cb])
+        assert err < TOL[prec], (gop, cb, isign, prec, err)
+
+
+def test_multi_rhs_apply_matches_single(setup):
+    dims, op, ctx = setup
+    V = int(np.prod(dims))
+    xs = np.stack([S.gaussian(dims, 100 + k).reshape(V, 12) for k in range(12)])
+    for prec in (G.PREC_DOUBLE, G.PREC_HALF):
+        for n in (4, 12):
+            many = ctx.apply(G.OP_MEO, xs[:n], +1, 1, prec)
+            for k in range(n):
+                one = ctx.apply(G.OP_MEO, xs[k], +1, 1, prec)[0]
+                assert np.array_equal(many[k], one), (prec, n, k)
+
+
+def test_repeatable_bitwise(setup):
+    dims, op, ctx = setup
+    x = S.gaussian(dims, 3)
+    a = ctx.apply(G.OP_MDAGM, x, +1, 1, G.PREC_DOUBLE)
+    b = ctx.apply(G.OP_MDAGM, x, +1, 1, G.PREC_DOUBLE)
+    assert np.array_equal(a, b)
+
+
+def _true_rel(op, psi, chi):
+    from oracle import oracle as O
+    r = chi - op.apply(O.OP_MEO, psi)
+    return np.sqrt(op.norm2(r) / op.norm2(chi))
+
+
+@pytest.mark.parametrize("solver,sloppy", [(G.SOLVER_CG, 0), (G.SOLVER_MIXED, G.PREC_HALF),
+                                           (G.SOLVER_MIXED, G.PREC_SINGLE), (G.SOLVER_RELIABLE_CG, G.PREC_HALF),
+                                           (G.SOLVER_RELIABLE_CG, G.PREC_SINGLE)],
+                         ids=["cg64", "mixed16", "mixed32", "rel16", "rel32"])
+def test_solvers_reach_1e10(setup, solver, sloppy):
+    from oracle import oracle as O
+    dims, op, ctx = setup
+    chi = S.z2_noise(dims, 11, cb=1).reshape(1, -1, 12)
+    psi, res, rc = ctx.solve(chi, solver=solver, sloppy_precision=sloppy, rsd_target=1e-10)
+    assert rc == 0 and res[0]["status"] == 0, res
+    true_rel = _true_rel(op, psi[0], chi[0])
+    assert true_rel <= 1e-10 * 1.05, (true_rel, res)
+    assert abs(res[0]["rel_resid"] - true_rel) < 1e-2 * true_rel
+    ref, _ = op.solve(chi[0], solver=O.SOLVER_CG, rsd=1e-12)
+    assert rel(psi[0], ref) < 1e-8
+
+
+def test_full_system_qprop(setup):
+    dims, op, ctx = setup
+    from oracle import oracle as O
+    chi = S.gaussian(dims, 21).reshape(1, -1, 12)
+    psi, res, rc = ctx.solve(chi, solver=G.SOLVER_MIXED, system=G.SYS_FULL, rsd_target=1e-10)
+    assert rc == 0
+    r = op.apply(O.OP_UNPREC, psi[0]) - chi[0]
+    full_rel = np.linalg.norm(r) / np.linalg.norm(chi[0])
+    assert full_rel < 1e-9, full_rel
+    assert abs(res[0]["rel_resid"] - full_rel) < 1e-2 * full_rel
+
+
+def test_mdagm_system(setup):
+    from oracle import oracle as O
+    dims, op, ctx = setup
+    chi = S.gaussian(dims, 31, cb=1).reshape(1, -1, 12)
+    psi, res, rc = ctx.solve(chi, solver=G.SOLVER_MIXED, system=G.SYS_MDAGM, rsd_target=1e-10)
+    assert rc == 0
+    r = chi[0] - op.apply(O.OP_MDAGM, psi[0])
+    assert np.sqrt(op.norm2(r) / op.norm2(chi[0])) <= 1.05e-10
+
+
+def test_multi_rhs_solve_point_sources(setup):
+    dims, op, ctx = setup
+    src = S.point_sources(dims).reshape(12, -1, 12)
+    psi, res, rc = ctx.solve(src, solver=G.SOLVER_MIXED, system=G.SYS_FULL, rsd_target=1e-10)
+    assert rc == 0
+    from oracle import oracle as O
+    for k in (0, 5, 11):
+        r = op.apply(O.OP_UNPREC, psi[k]) - src[k]
+        assert np.linalg.norm(r) / np.linalg.norm(src[k]) < 1e-9
