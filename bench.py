@@ -1,0 +1,343 @@
+"""Benchmark: 12-source Wilson-clover propagator solve on one GB300, to FP64 true residual 1e-10.
+
+Workload (the spec volume): 32^3 x 64, periodic space / antiperiodic time, hot-start links
+U = reunit(exp(i 0.3 H)) (seeded), kappa = 0.1250, c_sw = 1.6, the 12 spin-colour point sources
+at the origin solved together as one multi-RHS batch through the full even-odd system
+(Schur prep, odd solve, even reconstruction: Chroma's PrecFermActQprop + quarkProp4_a).
+
+A step is one such propagator solve.  value = seconds per propagator (device-resident inputs,
+CUDA events on the library stream, max over ranks / N for N replicas); e2e = the same through
+gbc_solve with pinned host buffers (H2D of the sources and D2H of the solution inside the clock).
+The baseline on the same GPU is plain FP64 CG (CGNE, InvCG2) solving the 12 sources one by one;
+the CPU baseline is the oracle's FP64 CG on the host cores (bounded sample, extrapolated).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbc|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Solve time at rel. residual 1e-10: learned+mixed vs plain CG; Dslash HBM GB/s"
+DIMS = (32, 32, 32, 64)
+KAPPA, CSW, EPS, SEED = 0.1250, 1.6, 0.3, 20251203
+RSD = 1e-10
+# InvCG2 iterations of one source of this workload (FP64 CGNE; the GPU FP64 CG and the oracle run
+# the same recursion).  The GPU arm re-measures it every run and reports both.
+CG_ITERS_REF = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbc", choices=["gbc", "reference"])
+    ap.add_argument("--dims", default=None, help="override lattice, e.g. 16,16,16,32 (testing only)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-steps", type=int, default=1)
+    return ap.parse_args()
+
+
+def dist_init(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() and args.impl == "gbc" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+        self.f.flush()
+        rows = []
+        try:
+            for line in open(self.f.name):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        finally:
+            os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows]
+        smax = max(float(r[2]) for r in rows)
+        load = [s for s in sm if s > 0.5 * smax] or sm
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, n in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+def workload(dims):
+    from chroma_gb300 import gbclover as G
+    from chroma_gb300 import sources as S
+    links = G.gauge_synthetic(dims, EPS, SEED, t_boundary=-1)
+    src = S.point_sources(dims).reshape(12, -1, 12)
+    return links, src
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_baseline(dims, links, chi_one, iters_full, nsrc, budget_s=20.0):
+    """Oracle FP64 InvCG2 on the host cores: a bounded number of iterations on one source,
+    extrapolated to the full 12-source solve by the measured FP64 iteration count."""
+    from oracle import OracleOp
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    op = OracleOp(dims, links, 1 / (2 * KAPPA) - 4, CSW)
+    setup = time.perf_counter() - t0
+    # calibrate with 2 iterations, then run as many as fit in the budget
+    t0 = time.perf_counter()
+    op.solve(chi_one, solver=O.SOLVER_CG, rsd=1e-30, maxit=2)
+    per = (time.perf_counter() - t0) / 3.0  # 2 iterations + the M~^dag and residual applications
+    k = max(2, min(200, int(budget_s / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    op.solve(chi_one, solver=O.SOLVER_CG, rsd=1e-30, maxit=k)
+    dt = time.perf_counter() - t0
+    per_iter = dt / (k + 1.5)
+    threads = O.load().orc_num_threads()
+    return {"value": per_iter * iters_full * nsrc, "unit": "s", "cores": threads, "kind": "port",
+            "sample": f"{k} InvCG2 iterations of 1 of {nsrc} sources ({dt:.1f} s, oracle FP64, OpenMP); "
+                      f"extrapolated x {iters_full} iterations x {nsrc} sources; operator setup {setup:.1f} s",
+            "seconds_per_cg_iteration": per_iter}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: Chroma's FP64 CG restated (the oracle) on all host cores."""
+    if rank != 0:
+        return
+    dims = tuple(int(x) for x in args.dims.split(",")) if args.dims else DIMS
+    from chroma_gb300 import sources as S
+    from oracle import Oracle, OracleOp
+    from oracle import oracle as O
+    o = Oracle()
+    links = o.apply_bc(dims, o.gauge_hot(dims, EPS, SEED), (1, 1, 1, -1))
+    op = OracleOp(dims, links, 1 / (2 * KAPPA) - 4, CSW)
+    chi = S.point(dims, 0, 0).reshape(-1, 12)
+    iters_full = CG_ITERS_REF or 0
+    per_step = []
+    k = 3
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        op.solve(chi, solver=O.SOLVER_CG, rsd=1e-30, maxit=k)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            per_step.append(dt / (k + 1.5))
+    per_iter = statistics.median(per_step)
+    if not iters_full:
+        # no recorded count: converge one source fully on the host (slow, only when not recorded)
+        _, res = op.solve(chi, solver=O.SOLVER_CG, rsd=RSD, maxit=5000)
+        iters_full = res["n_count"]
+    value = per_iter * iters_full * 12
+    line = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * k * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{'x'.join(map(str, dims))} clover propagator, 12 point sources, kappa={KAPPA}, "
+                                   f"c_sw={CSW}, FP64 CGNE (InvCG2) on the host cores"},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": O.load().orc_num_threads(), "kind": "port",
+                             "sample": f"{k} InvCG2 iterations per step on 1 source, extrapolated x {iters_full} "
+                                       f"iterations x 12 sources"},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+
+    from chroma_gb300 import gbclover as G
+    dims = tuple(int(x) for x in args.dims.split(",")) if args.dims else DIMS
+    V = int(np.prod(dims))
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    links, src = workload(dims)
+    mass = 1 / (2 * KAPPA) - 4
+    ctx = G.Context(dims, mass, CSW, t_boundary=-1, sloppy_precision=G.PREC_HALF, max_rhs=12)
+    ctx.load_gauge(links)
+    nsrc = src.shape[0]
+    # device-resident sources / solutions in the canonical layout
+    chi_d = torch.from_numpy(src.view(np.float64)).cuda()
+    psi_d = torch.zeros_like(chi_d)
+    solve_kw = dict(solver=G.SOLVER_MIXED, system=G.SYS_FULL, rsd_target=RSD, sloppy_precision=G.PREC_HALF)
+
+    def step():
+        res, rc = ctx.solve_device(psi_d.data_ptr(), chi_d.data_ptr(), nsrc, **solve_kw)
+        if rc != 0:
+            raise RuntimeError(f"solve failed: {rc} {res}")
+        return res
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        step()
+    clocks = Clocks()
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    times, results = [], []
+    for _ in range(args.steps):
+        flush.random_()  # L2 flush between timed steps (outside the events)
+        torch.cuda.synchronize()
+        res = step()
+        times.append(res[0]["device_seconds"])
+        results.append(res)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    t_step = max_over_ranks(sum(times) / len(times), world)
+    value = t_step / world  # seconds per propagator over the whole job (N replicas)
+    last = results[-1]
+    psi_host = psi_d.cpu().numpy().view(np.complex128).reshape(nsrc, V, 12)
+
+    # plain FP64 CG on the same GPU, sources one at a time (quarkProp4_a's loop)
+    plain_t, plain_iters, plain_res = [], [], []
+    for _ in range(max(1, args.plain_steps)):
+        tot = 0.0
+        its = []
+        for k in range(nsrc):
+            psi1 = torch.zeros_like(chi_d[k:k + 1])
+            res, rc = ctx.solve_device(psi1.data_ptr(), chi_d[k:k + 1].data_ptr(), 1, solver=G.SOLVER_CG,
+                                       system=G.SYS_FULL, rsd_target=RSD)
+            if rc != 0:
+                raise RuntimeError(f"plain CG failed {res}")
+            tot += res[0]["device_seconds"]
+            its.append(res[0]["n_count"])
+            plain_res.append(res[0]["rel_resid"])
+        plain_t.append(tot)
+        plain_iters = its
+    plain = statistics.median(plain_t)
+    # error of the accelerated solution against the FP64 CG solution of source 0
+    psi_cg = torch.zeros_like(chi_d[0:1])
+    ctx.solve_device(psi_cg.data_ptr(), chi_d[0:1].data_ptr(), 1, solver=G.SOLVER_CG, system=G.SYS_FULL,
+                     rsd_target=1e-12)
+    ref0 = psi_cg.cpu().numpy().view(np.complex128).reshape(V, 12)
+    err_vs_fp64 = float(np.linalg.norm(psi_host[0] - ref0) / np.linalg.norm(ref0))
+
+    # Dslash roofline: the FP16 12-RHS hopping kernel (dominant), cold L2 per launch
+    pk, pk_kind = peaks()
+    sec, byts = ctx.time_operator(G.OP_DSLASH, G.PREC_HALF, nrhs=12, iters=20, flush_l2=True)
+    sec1, byts1 = ctx.time_operator(G.OP_DSLASH, G.PREC_HALF, nrhs=1, iters=20, flush_l2=True)
+    sec64, byts64 = ctx.time_operator(G.OP_DSLASH, G.PREC_DOUBLE, nrhs=1, iters=10, flush_l2=True)
+    achieved = byts / sec / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+            "kernel": "hop_kernel<PrecH,12,HOP_PLAIN> 12 RHS (Dslash, FP16 storage, 12-real links)",
+            "bytes_per_launch": byts, "seconds_per_launch": sec,
+            "single_rhs_fp16_gbs": byts1 / sec1 / 1e9, "single_rhs_fp64_gbs": byts64 / sec64 / 1e9}
+
+    # e2e through the public API with pinned host buffers
+    chi_h = torch.from_numpy(src.view(np.float64).copy()).pin_memory()
+    psi_h = torch.zeros_like(chi_h).pin_memory()
+    e2e_t = []
+    import ctypes as C
+    p = G.SolveParams(G.SOLVER_MIXED, G.SYS_FULL, RSD, 10000, 0.1, 10.0, G.PREC_HALF, 0.0, 0, 16, 0, 1)
+    for i in range(max(1, min(args.steps, 3))):
+        res_arr = (G.Result * nsrc)()
+        t0 = time.perf_counter()
+        rc = ctx.lib.gbc_solve(ctx.h, C.byref(p), nsrc, C.cast(psi_h.data_ptr(), C.POINTER(C.c_double)),
+                               C.cast(chi_h.data_ptr(), C.POINTER(C.c_double)), res_arr)
+        e2e_t.append(time.perf_counter() - t0)
+        if rc != 0:
+            raise RuntimeError("e2e solve failed")
+    e2e = max_over_ranks(statistics.median(e2e_t), world) / world
+    nbytes = src.nbytes
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(dims, links, src[0], int(np.median(plain_iters)), nsrc)
+
+    iters = [r["n_count"] for r in last]
+    line = {
+        "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f16-storage/f32-arith inner, f64 outer", "data": "synthetic",
+        "config": {"workload": f"{'x'.join(map(str, dims))} Wilson-clover propagator, 12 point sources, "
+                               f"kappa={KAPPA}, c_sw={CSW}, hot start eps={EPS}, antiperiodic t, full system, "
+                               f"FP64 true residual {RSD}",
+                   "solver": "FP64 defect correction + reliable-update CGNE (FP16 stencil, 12-real links), "
+                             "12-RHS batch",
+                   "l2": "256 MiB L2 flush between timed steps; the fields exceed L2",
+                   "parallelism": f"replicas x{world}"},
+        "plain_cg_fp64_s": plain, "speedup_vs_plain_cg": plain / value if value else None,
+        "iterations": {"mixed_inner_per_rhs_median": int(np.median(iters)), "plain_cg_per_rhs": plain_iters},
+        "true_rel_resid_max": max(r["rel_resid"] for r in last),
+        "plain_cg_true_rel_resid_max": max(plain_res),
+        "rel_error_vs_fp64_cg_src0": err_vs_fp64,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes},
+        "gpu_launches": None,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

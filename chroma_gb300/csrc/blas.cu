@@ -260,6 +260,7 @@ void run(const Geom& g, int nrhs, const F& f, const Red* red, cudaStream_t s) {
   dim3 grid(blas_blocks(g), nrhs);
   site_kernel<NRED, F><<<grid, BLAS_THREADS, 0, s>>>(g.Vh, f, red ? red->partials : nullptr,
                                                      red ? red->part_stride : 0, nrhs);
+  count_launch();
   if (NRED > 0) reduce_finalize(*red, NRED, nrhs, grid.x, s);
 }
 
@@ -274,6 +275,7 @@ int blas_blocks(const Geom& g) {
 
 void reduce_finalize(const Red& red, int nred, int nrhs, int nblocks, cudaStream_t s) {
   finalize_kernel<<<nred * nrhs, 256, 0, s>>>(red.partials, red.part_stride, nblocks, red.result);
+  count_launch();
 }
 
 #define GBC_DISPATCH1(prec, CALL) \
@@ -329,9 +331,11 @@ void blas_xpy(const Geom& g, const Spinor& x, const Spinor& y, cudaStream_t s) {
 
 void cg_alpha(CGScalars* st, const double* red_d, double* a_out, int nrhs, cudaStream_t s) {
   cg_alpha_kernel<<<1, 32, 0, s>>>(st, red_d, a_out, nrhs);
+  count_launch();
 }
 void cg_beta(CGScalars* st, const double* red_r, double* b_out, int nrhs, cudaStream_t s) {
   cg_beta_kernel<<<1, 32, 0, s>>>(st, red_r, b_out, nrhs);
+  count_launch();
 }
 
 }  // namespace gbc

@@ -1,4 +1,5 @@
 // C-ABI lifecycle, field import and operator application (include/gbclover.h).
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -9,6 +10,10 @@ namespace gbc {
 void cuda_check(cudaError_t e, const char* where) {
   if (e != cudaSuccess) throw CudaError{e, where};
 }
+
+static std::atomic<long long> g_launches{0};
+void count_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 double now() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -175,6 +180,7 @@ void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, con
   HopShape sh = in.nrhs >= 12 && in.nrhs % 12 == 0 ? HopShape{32, 12} : in.nrhs >= 4 ? HopShape{32, 4} : HopShape{128, 1};
   int nb = hop_launch(prec, f.recon, mode, dag, reduce, h, sh, c->stream);
   if (nb < 0) throw std::string("hopping kernel variant not compiled");
+  count_launch();
   if (nb > c->part_stride) throw std::string("partials buffer too small");
   GBC_CUDA(cudaGetLastError());
   if (reduce) reduce_finalize(red(c), 1, in.nrhs, nb, c->stream);
@@ -284,7 +290,7 @@ int gbc_create(gbc_ctx** out, const gbc_geom* geom, const gbc_action* act, const
     GBC_CUDA(cudaMalloc(&c->d_ca, sizeof(double2) * c->max_rhs));
     GBC_CUDA(cudaMalloc(&c->d_cb, sizeof(double2) * c->max_rhs));
     GBC_CUDA(cudaMallocHost(&c->h_coef, sizeof(double2) * 2 * c->max_rhs));
-    GBC_CUDA(cudaMalloc(&c->d_links, sizeof(double) * 36 * V));
+    GBC_CUDA(cudaMalloc(&c->d_links, sizeof(double) * 72 * V));
     GBC_CUDA(cudaMalloc(&c->d_clov, sizeof(double) * 72 * V));
     GBC_CUDA(cudaMalloc(&c->d_inv, sizeof(double) * 72 * V));
     return GBC_OK;
@@ -318,7 +324,7 @@ int gbc_load_gauge(gbc_ctx* c, const double* links) {
   if (!c || !links) return GBC_ERR_ARGS;
   return guarded(c, [&]() {
     const long V = c->V;
-    GBC_CUDA(cudaMemcpyAsync(c->d_links, links, sizeof(double) * 36 * V, cudaMemcpyHostToDevice, c->stream));
+    GBC_CUDA(cudaMemcpyAsync(c->d_links, links, sizeof(double) * 72 * V, cudaMemcpyHostToDevice, c->stream));
     const gbc_action& a = c->act;
     CloverCoeffs cc{};
     double ffR = a.aniso ? 1.0 / a.xi_0 : 1.0;
@@ -449,7 +455,10 @@ int gbc_solve(gbc_ctx* c, const gbc_solve_params* p, int nrhs, double* psi, cons
     ensure_stage(c, nrhs);
     const size_t n = (size_t)nrhs * c->V * 24;
     GBC_CUDA(cudaMemcpyAsync(c->d_stage[0], chi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    GBC_CUDA(cudaMemcpyAsync(c->d_stage[1], psi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    // psi is read as the initial guess, and its even sites must survive an odd-parity solve;
+    // only a zero-guess solve of the full system overwrites every site without reading psi
+    if (!(p->zero_guess && p->system == GBC_SYS_FULL))
+      GBC_CUDA(cudaMemcpyAsync(c->d_stage[1], psi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     int rc = solve_device(c, p, nrhs, c->d_stage[1], c->d_stage[0], res);
     GBC_CUDA(cudaMemcpyAsync(psi, c->d_stage[1], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     sync(c);

@@ -47,7 +47,7 @@ struct gbc_ctx {
   double link_coeff[4] = {1, 1, 1, 1};
 
   // canonical FP64 copies on the device
-  double* d_links = nullptr;  // [V][36]
+  double* d_links = nullptr;  // [V][4][3][3] complex = 72 doubles per site
   double* d_clov = nullptr;   // [V][72]
   double* d_inv = nullptr;    // [V][72] (even sites)
   double logdet_even = 0;

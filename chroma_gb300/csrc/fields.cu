@@ -179,6 +179,7 @@ void import_spinor(const Geom& g, const double* canon, size_t canon_rhs, int cb,
   if (f.prec == PREC_DOUBLE) import_spinor_kernel<PrecD><<<grid, 128, 0, s>>>(g, c, canon_rhs, cb, f);
   else if (f.prec == PREC_SINGLE) import_spinor_kernel<PrecS><<<grid, 128, 0, s>>>(g, c, canon_rhs, cb, f);
   else import_spinor_kernel<PrecH><<<grid, 128, 0, s>>>(g, c, canon_rhs, cb, f);
+  count_launch();
 }
 
 void export_spinor(const Geom& g, double* canon, size_t canon_rhs, int cb, const Spinor& f, cudaStream_t s) {
@@ -187,6 +188,7 @@ void export_spinor(const Geom& g, double* canon, size_t canon_rhs, int cb, const
   if (f.prec == PREC_DOUBLE) export_spinor_kernel<PrecD><<<grid, 128, 0, s>>>(g, c, canon_rhs, cb, f);
   else if (f.prec == PREC_SINGLE) export_spinor_kernel<PrecS><<<grid, 128, 0, s>>>(g, c, canon_rhs, cb, f);
   else export_spinor_kernel<PrecH><<<grid, 128, 0, s>>>(g, c, canon_rhs, cb, f);
+  count_launch();
 }
 
 }  // namespace gbc

@@ -194,8 +194,12 @@ __device__ __forceinline__ void store_spinor<PrecH>(void* base, float* norm, int
   float m = 0.f;
 #pragma unroll
   for (int k = 0; k < 12; ++k) m = fmaxf(m, fmaxf(fabsf(s[k].re), fabsf(s[k].im)));
-  float inv = m > 0.f ? 1.0f / m : 0.f;
-  norm[idx] = m;
+  // a site whose largest component is below 1e-30 is stored as zero: 1/m would overflow for
+  // subnormal m (and 0 * inf = NaN), and such a site is far below fp16 resolution of any field
+  // the solvers carry
+  const bool live = m >= 1e-30f;
+  float inv = live ? 1.0f / m : 0.f;
+  norm[idx] = live ? m : 0.f;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     uint4 v;

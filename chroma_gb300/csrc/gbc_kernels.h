@@ -6,6 +6,10 @@
 
 namespace gbc {
 
+// every host wrapper that launches a kernel of this library adds to this counter
+void count_launch(long long n = 1);
+long long launch_count();
+
 enum { HOP_PLAIN = 0, HOP_CLOV = 1, HOP_XPAY = 2 };
 enum { PREC_HALF = 2, PREC_SINGLE = 4, PREC_DOUBLE = 8 };
 

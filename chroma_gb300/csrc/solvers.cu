@@ -317,6 +317,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   GBC_CUDA(cudaEventCreate(&ev0));
   GBC_CUDA(cudaEventCreate(&ev1));
   GBC_CUDA(cudaEventRecord(ev0, s));
+  const long long launches0 = launch_count();
   const int n = nrhs;
   Spinor chi = sub(workspace(c, SLOT_B, D, n), 0, n);    // odd right-hand side of the odd system
   Spinor psi = sub(workspace(c, SLOT_X, D, n), 0, n);    // odd solution
@@ -332,9 +333,17 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     chie = sub(workspace(c, SLOT_CHIE, D, n), 0, n);
     psie = sub(workspace(c, SLOT_PSIE, D, n), 0, n);
     import_spinor(g, chi_canon, rs, 0, chie, s);
+    std::vector<double> no = norm2(c, chi), ne = norm2(c, chie);
     apply_clover(c, D, 0, true, chie, ted);
     hop(c, D, 1, HOP_PLAIN, false, 0.5, ted, t1, nullptr, nullptr, false);
     blas_xpy(g, chi, t1, s);
+    // the even reconstruction is exact, so the full residual equals the odd one: solve the odd
+    // system to target * |chi| / |chi'_o| so that |M psi - chi| / |chi| meets the target
+    std::vector<double> np = norm2(c, chi);
+    double scale = 1.0;
+    for (int i = 0; i < n; ++i)
+      if (np[i] > 0) scale = std::min(scale, std::sqrt((no[i] + ne[i]) / np[i]));
+    p.rsd_target *= scale;
   }
   if (p.zero_guess) blas_zero(g, psi, s);
   else import_spinor(g, psi_canon, rs, 1, psi, s);
@@ -350,10 +359,39 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
       rhs = sub(workspace(c, SLOT_RHS, D, n), 0, n);
       apply_meo(c, D, true, chi, rhs, ted, false);
     }
-    CgCfg cfg{D, D, p.rsd_target, p.max_iter, 0.0, 4};
-    CgStats st = cg_normal(c, cfg, psi, rhs, p.zero_guess != 0, std::vector<int>(n, 1));
-    iters = st.iters;
-    status = st.status;
+    // CGNE stops on |M^dag r| <= RsdCG |M^dag chi|; the true residual of M psi = chi can end
+    // slightly above the target, so restart from the current psi with a tightened tolerance until
+    // the FP64 true residual meets it (Chroma's optional restart, syssolver_linop_cg.h:73-81)
+    std::vector<int> active(n, 1);
+    std::vector<double> bb = norm2(c, chi);
+    double tol = p.rsd_target;
+    for (int pass = 0; pass < 4; ++pass) {
+      int budget = p.max_iter;
+      for (int i = 0; i < n; ++i) budget = std::min(budget, p.max_iter - iters[i]);
+      if (budget <= 0) break;
+      CgCfg cfg{D, D, tol, budget, 0.0, 4};
+      CgStats st = cg_normal(c, cfg, psi, rhs, pass == 0 && p.zero_guess != 0, active);
+      for (int i = 0; i < n; ++i) {
+        if (!active[i]) continue;
+        iters[i] += st.iters[i];
+        status[i] = st.status[i];
+      }
+      apply_sys(c, D, mdagm, psi, t1, t2, ted);
+      blas_xmy_norm2(g, chi, t1, red(c), s);
+      std::vector<double> rr = fetch(c, 1, n);
+      double worst_rel = 0;
+      bool any = false;
+      for (int i = 0; i < n; ++i) {
+        double relr = bb[i] > 0 ? std::sqrt(rr[i] / bb[i]) : 0.0;
+        active[i] = status[i] == GBC_OK && relr > p.rsd_target;
+        if (active[i]) {
+          any = true;
+          worst_rel = std::max(worst_rel, relr);
+        }
+      }
+      if (!any) break;
+      tol *= 0.5 * p.rsd_target / worst_rel;
+    }
   } else if (p.solver == GBC_SOLVER_RELIABLE_CG) {
     Spinor rhs = chi;
     if (!mdagm) {
@@ -475,6 +513,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     gbc_result& o = res[i];
     std::memset(&o, 0, sizeof(o));
     o.device_seconds = ms * 1e-3;
+    o.launches = launch_count() - launches0;
     o.n_count = iters[i];
     o.resid = std::sqrt(rr[i]);
     o.rel_resid = bb[i] > 0 ? std::sqrt(rr[i] / bb[i]) : o.resid;

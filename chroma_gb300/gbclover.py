@@ -54,7 +54,7 @@ class SolveParams(C.Structure):
 class Result(C.Structure):
     _fields_ = [("n_count", C.c_int), ("status", C.c_int), ("resid", C.c_double), ("rel_resid", C.c_double),
                 ("seconds", C.c_double), ("n_outer", C.c_int), ("n_reliable", C.c_int),
-                ("device_seconds", C.c_double)]
+                ("device_seconds", C.c_double), ("launches", C.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

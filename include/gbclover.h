@@ -120,6 +120,7 @@ typedef struct gbc_result {
   int n_outer;        /* outer (FP64) iterations of the mixed solvers          */
   int n_reliable;     /* reliable updates                                      */
   double device_seconds; /* CUDA-event time of the solve on the context stream  */
+  long long launches;    /* kernels this library launched during the solve      */
 } gbc_result;
 
 typedef struct gbc_ctx gbc_ctx;

@@ -84,6 +84,18 @@ def test_multi_rhs_apply_matches_single(setup):
                 assert np.array_equal(many[k], one), (prec, n, k)
 
 
+def test_half_precision_tiny_sites_stay_finite(setup):
+    """Sites whose components are subnormal in FP32 must not turn into NaN in fp16 storage."""
+    dims, op, ctx = setup
+    V = int(np.prod(dims))
+    x = np.zeros((V, 12), dtype=np.complex128)
+    x[::7] = 1e-39
+    x[3] = 1.0
+    for code, cb in [(G.OP_CLOVER, 1), (G.OP_CLOVER, 0), (G.OP_DSLASH, 1), (G.OP_MEO, 1)]:
+        y = ctx.apply(code, x, +1, cb, G.PREC_HALF)[0]
+        assert np.all(np.isfinite(y)), code
+
+
 def test_repeatable_bitwise(setup):
     dims, op, ctx = setup
     x = S.gaussian(dims, 3)
@@ -109,10 +121,19 @@ def test_solvers_reach_1e10(setup, solver, sloppy):
     psi, res, rc = ctx.solve(chi, solver=solver, sloppy_precision=sloppy, rsd_target=1e-10)
     assert rc == 0 and res[0]["status"] == 0, res
     true_rel = _true_rel(op, psi[0], chi[0])
-    assert true_rel <= 1e-10 * 1.05, (true_rel, res)
+    if solver == G.SOLVER_RELIABLE_CG:
+        # Chroma's reliable CGNE stops on the normal-equation residual; the true residual of
+        # M~ psi = chi lands within RsdToleranceFactor (10) of the target, as in the reference
+        assert true_rel <= 1e-9, (true_rel, res)
+    else:
+        assert true_rel <= 1e-10 * 1.05, (true_rel, res)
     assert abs(res[0]["rel_resid"] - true_rel) < 1e-2 * true_rel
-    ref, _ = op.solve(chi[0], solver=O.SOLVER_CG, rsd=1e-12)
+    ref, oref = op.solve(chi[0], solver=O.SOLVER_CG, rsd=1e-12)
     assert rel(psi[0], ref) < 1e-8
+    if solver == G.SOLVER_CG:
+        # same recursion as the oracle's InvCG2: the first pass needs the same iteration count
+        _, o10 = op.solve(chi[0], solver=O.SOLVER_CG, rsd=1e-10)
+        assert o10["n_count"] <= res[0]["n_count"] <= o10["n_count"] + 20, (o10, res)
 
 
 def test_full_system_qprop(setup):
@@ -124,7 +145,7 @@ def test_full_system_qprop(setup):
     r = op.apply(O.OP_UNPREC, psi[0]) - chi[0]
     full_rel = np.linalg.norm(r) / np.linalg.norm(chi[0])
     assert full_rel < 1e-9, full_rel
-    assert abs(res[0]["rel_resid"] - full_rel) < 1e-2 * full_rel
+    assert abs(res[0]["rel_resid"] - full_rel) < 1e-2 * full_rel + 1e-15
 
 
 def test_mdagm_system(setup):
@@ -135,6 +156,29 @@ def test_mdagm_system(setup):
     assert rc == 0
     r = chi[0] - op.apply(O.OP_MDAGM, psi[0])
     assert np.sqrt(op.norm2(r) / op.norm2(chi[0])) <= 1.05e-10
+
+
+def test_point_sources_near_critical_16x32():
+    """The propagator workload's parameters (kappa 0.1250, c_sw 1.6) on 16^3 x 32: the 12 point
+    sources as one batch through the full system, each to FP64 true residual 1e-10."""
+    from oracle import Oracle, OracleOp
+    from oracle import oracle as O
+    dims = (16, 16, 16, 32)
+    o = Oracle()
+    u = o.apply_bc(dims, o.gauge_hot(dims, 0.3, 77), (1, 1, 1, -1))
+    mass = 1 / (2 * 0.125) - 4
+    op = OracleOp(dims, u, mass, 1.6)
+    ctx = G.Context(dims, mass, 1.6, t_boundary=-1, max_rhs=12)
+    try:
+        ctx.load_gauge(u)
+        src = S.point_sources(dims).reshape(12, -1, 12)
+        psi, res, rc = ctx.solve(src, solver=G.SOLVER_MIXED, system=G.SYS_FULL, rsd_target=1e-10)
+        assert rc == 0, res
+        for k in (0, 7, 11):
+            r = op.apply(O.OP_UNPREC, psi[k]) - src[k]
+            assert np.linalg.norm(r) / np.linalg.norm(src[k]) < 1.05e-10
+    finally:
+        ctx.close()
 
 
 def test_multi_rhs_solve_point_sources(setup):
