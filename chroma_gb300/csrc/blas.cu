@@ -78,10 +78,12 @@ struct Norm2F {
   __device__ void operator()(int idx, int r, double* acc) const {
     cplx<typename P::real> a[12];
     ld<P>(a, x, idx, r);
-    double s = 0.0;
+    // site sums in the field's compute precision, running sums in FP64
+    using T = typename P::real;
+    T s = 0;
 #pragma unroll
-    for (int k = 0; k < 12; ++k) s += (double)a[k].re * a[k].re + (double)a[k].im * a[k].im;
-    acc[0] += s;
+    for (int k = 0; k < 12; ++k) s = fmadd(a[k].re, a[k].re, fmadd(a[k].im, a[k].im, s));
+    acc[0] += (double)s;
   }
 };
 
@@ -93,14 +95,16 @@ struct CdotF {
     cplx<typename PY::real> b[12];
     ld<PX>(a, x, idx, r);
     ld<PY>(b, y, idx, r);
-    double re = 0.0, im = 0.0;
+    using T = typename std::conditional<std::is_same<PX, PrecD>::value || std::is_same<PY, PrecD>::value, double,
+                                        float>::type;
+    T re = 0, im = 0;
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
-      re += (double)a[k].re * b[k].re + (double)a[k].im * b[k].im;
-      im += (double)a[k].re * b[k].im - (double)a[k].im * b[k].re;
+      re = fmadd((T)a[k].re, (T)b[k].re, fmadd((T)a[k].im, (T)b[k].im, re));
+      im = fmadd((T)a[k].re, (T)b[k].im, fmadd(-(T)a[k].im, (T)b[k].re, im));
     }
-    acc[0] += re;
-    acc[1] += im;
+    acc[0] += (double)re;
+    acc[1] += (double)im;
   }
 };
 
@@ -141,18 +145,18 @@ struct CgUpdateF {
     ld<PO>(ps, p, idx, rr);
     ld<PO>(qs, q, idx, rr);
     const T al = (T)a[rr];
-    double s = 0.0;
+    T s = 0;
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
       xs[k].re = fmadd(al, (T)ps[k].re, xs[k].re);
       xs[k].im = fmadd(al, (T)ps[k].im, xs[k].im);
       rs[k].re = fmadd(-al, (T)qs[k].re, rs[k].re);
       rs[k].im = fmadd(-al, (T)qs[k].im, rs[k].im);
-      s += (double)rs[k].re * rs[k].re + (double)rs[k].im * rs[k].im;
+      s = fmadd(rs[k].re, rs[k].re, fmadd(rs[k].im, rs[k].im, s));
     }
     st<PA>(x, idx, rr, xs);
     st<PA>(r, idx, rr, rs);
-    acc[0] += s;
+    acc[0] += (double)s;
   }
 };
 
@@ -185,14 +189,14 @@ struct XmyNormF {
     cplx<typename P::real> xs[12], ys[12];
     ld<P>(xs, x, idx, r);
     ld<P>(ys, y, idx, r);
-    double s = 0.0;
+    typename P::real s = 0;
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
       ys[k] = xs[k] - ys[k];
-      s += (double)ys[k].re * ys[k].re + (double)ys[k].im * ys[k].im;
+      s = fmadd(ys[k].re, ys[k].re, fmadd(ys[k].im, ys[k].im, s));
     }
     st<P>(y, idx, r, ys);
-    acc[0] += s;
+    acc[0] += (double)s;
   }
 };
 

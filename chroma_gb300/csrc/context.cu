@@ -144,9 +144,63 @@ void free_ctx_memory(gbc_ctx* c) {
   if (c->d_cg) cudaFree(c->d_cg);
   for (int i = 0; i < 2; ++i)
     if (c->d_stage[i]) cudaFree(c->d_stage[i]);
+  if (c->d_kpartials) cudaFree(c->d_kpartials);
+  if (c->d_kresult) cudaFree(c->d_kresult);
+  if (c->d_kcoef) cudaFree(c->d_kcoef);
+  if (c->h_kresult) cudaFreeHost(c->h_kresult);
+  if (c->h_kcoef) cudaFreeHost(c->h_kcoef);
   if (c->h_result) cudaFreeHost(c->h_result);
   if (c->h_cg) cudaFreeHost(c->h_cg);
   if (c->h_coef) cudaFreeHost(c->h_coef);
+}
+
+// Autotuner: the first launch of each (precision, mode, sign, reduction, nrhs) times every compiled
+// shape (one warm-up and three timed launches, CUDA events on the context stream; the launches are
+// idempotent, out never aliases in) and keeps the fastest for the life of the context.  The
+// choices are listed in gbc_last_error-style text by gbc_tune_report; GBC_AUTOTUNE=0 switches it
+// off and uses a fixed shape.
+static int default_shape(int nrhs) {
+  if (nrhs >= 12 && nrhs % 12 == 0) return 5;
+  if (nrhs >= 4) return 3;
+  return 1;
+}
+
+int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce, const HopArgs& h) {
+  const long key = ((((long)pidx(prec) * 4 + mode) * 2 + (dag ? 1 : 0)) * 2 + (reduce ? 1 : 0)) * 64 + h.nrhs;
+  auto it = c->tuned.find(key);
+  if (it != c->tuned.end()) return it->second;
+  int best = default_shape(h.nrhs);
+  if (c->autotune) {
+    cudaEvent_t e0, e1;
+    GBC_CUDA(cudaEventCreate(&e0));
+    GBC_CUDA(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    for (int si = 0; si < kNumHopShapes; ++si) {
+      const HopShape sh = kHopShapes[si];
+      if (sh.nrb > 1 && sh.nrb > h.nrhs) continue;  // a block would be mostly idle
+      if (hop_launch(prec, recon, mode, dag, reduce, h, sh, c->stream) < 0) continue;
+      GBC_CUDA(cudaEventRecord(e0, c->stream));
+      for (int k = 0; k < 3; ++k) hop_launch(prec, recon, mode, dag, reduce, h, sh, c->stream);
+      GBC_CUDA(cudaEventRecord(e1, c->stream));
+      GBC_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      GBC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = si;
+      }
+    }
+    count_launch(4LL * kNumHopShapes);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    char line[160];
+    snprintf(line, sizeof line, "prec=%d mode=%d dag=%d reduce=%d nrhs=%d -> tx=%d nrb=%d minb=%d (%.1f us)\n", prec,
+             mode, dag ? 1 : 0, reduce ? 1 : 0, h.nrhs, kHopShapes[best].tx, kHopShapes[best].nrb,
+             kHopShapes[best].minb, best_ms / 3 * 1e3);
+    c->tune_log += line;
+  }
+  c->tuned[key] = best;
+  return best;
 }
 
 void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, const Spinor& in, const Spinor& out,
@@ -177,7 +231,7 @@ void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, con
   h.twist = twist;
   h.partials = c->d_partials;
   h.part_stride = c->part_stride;
-  HopShape sh = in.nrhs >= 12 && in.nrhs % 12 == 0 ? HopShape{32, 12} : in.nrhs >= 4 ? HopShape{32, 4} : HopShape{128, 1};
+  const HopShape sh = kHopShapes[tuned_shape(c, prec, f.recon, mode, dag, reduce, h)];
   int nb = hop_launch(prec, f.recon, mode, dag, reduce, h, sh, c->stream);
   if (nb < 0) throw std::string("hopping kernel variant not compiled");
   count_launch();
@@ -244,6 +298,8 @@ const char* gbc_strerror(int s) {
 
 const char* gbc_last_error(gbc_ctx* c) { return c ? c->err.c_str() : ""; }
 
+const char* gbc_tune_report(gbc_ctx* c) { return c ? c->tune_log.c_str() : ""; }
+
 int gbc_create(gbc_ctx** out, const gbc_geom* geom, const gbc_action* act, const gbc_opts* opts) {
   if (!out || !geom || !act) return GBC_ERR_ARGS;
   *out = nullptr;
@@ -271,6 +327,8 @@ int gbc_create(gbc_ctx** out, const gbc_geom* geom, const gbc_action* act, const
       c->opts.sloppy_precision = GBC_PREC_HALF;
     if (c->opts.sloppy_reconstruct != 12 && c->opts.sloppy_reconstruct != 18) c->opts.sloppy_reconstruct = 12;
     c->max_rhs = c->opts.max_rhs > 0 ? c->opts.max_rhs : 12;
+    const char* at = getenv("GBC_AUTOTUNE");
+    c->autotune = !(at && at[0] == '0');
     if (c->max_rhs > 32) throw std::string("max_rhs above 32");
     if (act->aniso) {
       for (int m = 0; m < 4; ++m)
@@ -290,6 +348,12 @@ int gbc_create(gbc_ctx** out, const gbc_geom* geom, const gbc_action* act, const
     GBC_CUDA(cudaMalloc(&c->d_ca, sizeof(double2) * c->max_rhs));
     GBC_CUDA(cudaMalloc(&c->d_cb, sizeof(double2) * c->max_rhs));
     GBC_CUDA(cudaMallocHost(&c->h_coef, sizeof(double2) * 2 * c->max_rhs));
+    c->kpart_stride = blas_blocks(g);
+    GBC_CUDA(cudaMalloc(&c->d_kpartials, sizeof(double) * 66 * c->max_rhs * (size_t)c->kpart_stride));
+    GBC_CUDA(cudaMalloc(&c->d_kresult, sizeof(double) * 66 * c->max_rhs));
+    GBC_CUDA(cudaMallocHost(&c->h_kresult, sizeof(double) * 66 * c->max_rhs));
+    GBC_CUDA(cudaMalloc(&c->d_kcoef, sizeof(double2) * 33 * c->max_rhs));
+    GBC_CUDA(cudaMallocHost(&c->h_kcoef, sizeof(double2) * 33 * c->max_rhs));
     GBC_CUDA(cudaMalloc(&c->d_links, sizeof(double) * 72 * V));
     GBC_CUDA(cudaMalloc(&c->d_clov, sizeof(double) * 72 * V));
     GBC_CUDA(cudaMalloc(&c->d_inv, sizeof(double) * 72 * V));

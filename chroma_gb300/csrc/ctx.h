@@ -69,12 +69,26 @@ struct gbc_ctx {
   double2* d_cb = nullptr;
   double2* h_coef = nullptr;  // pinned, 2 * max_rhs
 
+  // block-vector reductions of the flexible GMRES: partials [2*33][max_rhs][blas blocks],
+  // results [2*33][max_rhs], coefficients [33][max_rhs] (device + pinned host mirrors)
+  double* d_kpartials = nullptr;
+  int kpart_stride = 0;
+  double* d_kresult = nullptr;
+  double* h_kresult = nullptr;
+  double2* d_kcoef = nullptr;
+  double2* h_kcoef = nullptr;
+
   // canonical staging buffers on the device (2 x max_rhs x V x 24 doubles)
   double* d_stage[2] = {nullptr, nullptr};
   size_t stage_cap = 0;
 
   // workspace spinors keyed by slot
   std::map<int, gbc::Spinor> ws;
+
+  // autotuned hopping-kernel shapes, keyed by (precision, mode, dagger, reduce, nrhs)
+  std::map<long, int> tuned;
+  bool autotune = true;
+  std::string tune_log;
 
   // learned preconditioner (opaque, owned by precond.cu)
   void* precond = nullptr;
@@ -102,6 +116,8 @@ double now();
 
 // ---- learned preconditioner (precond.cu) ----------------------------------------------------
 void precond_free(gbc_ctx* c);
+// out ~= M~^-1 in (odd checkerboard fields, same precision, nrhs right-hand sides)
+void precond_apply(gbc_ctx* c, const Spinor& in, const Spinor& out);
 
 // ---- solvers (solvers.cu) -------------------------------------------------------------------
 int solve_device(gbc_ctx* c, const gbc_solve_params* p, int nrhs, double* psi_canon, const double* chi_canon,

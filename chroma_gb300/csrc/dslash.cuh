@@ -130,13 +130,171 @@ __device__ __forceinline__ void hop_dir(cplx<typename P::real> (&acc)[12], const
   }
 }
 
-template <typename P, int RECON, int MODE, bool DAG, bool REDUCE, int TX, int NRB>
-__global__ void __launch_bounds__(TX * NRB) hop_kernel(const HopArgs a) {
+// ---- FP32-arithmetic path on packed float2 instructions (FFMA2/FADD2/FMUL2 of sm_100+) ----------
+// A complex number is one float2; u*h = (ur, ur)*h + (-ui, ui)*swap(h), so every complex
+// multiply-add is two FFMA2 and every complex add one FADD2: half the instructions of scalar code.
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 f2addi(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.y, b.x)); }  // a + i b
+__device__ __forceinline__ float2 f2subi(float2 a, float2 b) { return __fadd2_rn(a, make_float2(b.y, -b.x)); }  // a - i b
+
+template <typename P>
+__device__ __forceinline__ void load_spinor_f2(float2 (&s)[12], float& n, const void* base, const float* norm, int idx,
+                                               int stride) {
+  if constexpr (std::is_same<P, PrecS>::value) {
+    const float4* p = reinterpret_cast<const float4*>(base);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      float4 v = ldg(p + (size_t)k * stride + idx);
+      s[2 * k] = make_float2(v.x, v.y);
+      s[2 * k + 1] = make_float2(v.z, v.w);
+    }
+    n = 1.0f;
+  } else {
+    const uint4* p = reinterpret_cast<const uint4*>(base);
+    n = ldg(norm + idx);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      uint4 v = ldg(p + (size_t)k * stride + idx);
+      s[4 * k + 0] = h2f(v.x);
+      s[4 * k + 1] = h2f(v.y);
+      s[4 * k + 2] = h2f(v.z);
+      s[4 * k + 3] = h2f(v.w);
+    }
+  }
+}
+
+// top half of (1 + S gamma_mu) psi on packed complex values
+template <int MU, int S>
+__device__ __forceinline__ void project_f2(float2 (&h)[2][3], const float2 (&p)[12]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float2 p0 = p[c], p1 = p[3 + c], p2 = p[6 + c], p3 = p[9 + c];
+    if constexpr (MU == 0) {
+      h[0][c] = S > 0 ? f2addi(p0, p3) : f2subi(p0, p3);
+      h[1][c] = S > 0 ? f2addi(p1, p2) : f2subi(p1, p2);
+    } else if constexpr (MU == 1) {
+      h[0][c] = S > 0 ? f2sub(p0, p3) : f2add(p0, p3);
+      h[1][c] = S > 0 ? f2add(p1, p2) : f2sub(p1, p2);
+    } else if constexpr (MU == 2) {
+      h[0][c] = S > 0 ? f2addi(p0, p2) : f2subi(p0, p2);
+      h[1][c] = S > 0 ? f2subi(p1, p3) : f2addi(p1, p3);
+    } else {
+      h[0][c] = S > 0 ? f2add(p0, p2) : f2sub(p0, p2);
+      h[1][c] = S > 0 ? f2add(p1, p3) : f2sub(p1, p3);
+    }
+  }
+}
+
+// acc_top += uh, acc_bot += S B uh (same B tables as reconstruct<>)
+template <int MU, int S>
+__device__ __forceinline__ void reconstruct_f2(float2 (&acc)[12], const float2 (&uh)[2][3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float2 a = uh[0][c], b = uh[1][c];
+    acc[c] = f2add(acc[c], a);
+    acc[3 + c] = f2add(acc[3 + c], b);
+    if constexpr (MU == 0) {
+      acc[6 + c] = S > 0 ? f2subi(acc[6 + c], b) : f2addi(acc[6 + c], b);
+      acc[9 + c] = S > 0 ? f2subi(acc[9 + c], a) : f2addi(acc[9 + c], a);
+    } else if constexpr (MU == 1) {
+      acc[6 + c] = S > 0 ? f2add(acc[6 + c], b) : f2sub(acc[6 + c], b);
+      acc[9 + c] = S > 0 ? f2sub(acc[9 + c], a) : f2add(acc[9 + c], a);
+    } else if constexpr (MU == 2) {
+      acc[6 + c] = S > 0 ? f2subi(acc[6 + c], a) : f2addi(acc[6 + c], a);
+      acc[9 + c] = S > 0 ? f2addi(acc[9 + c], b) : f2subi(acc[9 + c], b);
+    } else {
+      acc[6 + c] = S > 0 ? f2add(acc[6 + c], a) : f2sub(acc[6 + c], a);
+      acc[9 + c] = S > 0 ? f2add(acc[9 + c], b) : f2sub(acc[9 + c], b);
+    }
+  }
+}
+
+// uh = U h (ADJ: U^dag h) for the two half-spinor colour vectors, h scaled by n
+template <bool ADJ>
+__device__ __forceinline__ void matvec_f2(float2 (&uh)[2][3], const cplx<float> (&u)[9], const float2 (&h)[2][3]) {
+  float2 hs[2][3];
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) hs[s][c] = make_float2(h[s][c].y, h[s][c].x);
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      // element multiplying h[.][k] in row r: U[r][k] or conj(U[k][r])
+      const cplx<float> e = ADJ ? u[3 * k + r] : u[3 * r + k];
+      const float2 A = make_float2(e.re, e.re);
+      const float2 B = ADJ ? make_float2(e.im, -e.im) : make_float2(-e.im, e.im);
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        float2 v = k == 0 ? __fmul2_rn(A, h[s][0]) : __ffma2_rn(A, h[s][k], uh[s][r]);
+        uh[s][r] = __ffma2_rn(B, hs[s][k], v);
+      }
+    }
+  }
+}
+
+// fp16 spinors are stored divided by their site norm: scale the projected half spinor back
+template <typename P>
+__device__ __forceinline__ void scale_f2(float2 (&h)[2][3], float n) {
+  if constexpr (std::is_same<P, PrecH>::value) {
+    const float2 nn = make_float2(n, n);
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) h[s][c] = __fmul2_rn(h[s][c], nn);
+  }
+}
+
+template <typename P, int RECON, int MU, bool DAG>
+__device__ __forceinline__ void hop_dir_f2(float2 (&acc)[12], const HopArgs& a, const Coord& c, int idx,
+                                           const char* in, const float* in_norm) {
+  constexpr int SF = DAG ? +1 : -1;
+  constexpr int SB = DAG ? -1 : +1;
+  const Geom& g = a.g;
+  float2 s[12], h[2][3], uh[2][3];
+  cplx<float> u[9];
+  float n;
+  {
+    Coord nb = c;
+    nb.x[MU] = c.x[MU] + 1 == g.L[MU] ? 0 : c.x[MU] + 1;
+    const int ni = cb_index(g, nb);
+    load_spinor_f2<P>(s, n, in, in_norm, ni, g.stride);
+    project_f2<MU, SF>(h, s);
+    scale_f2<P>(h, n);
+    const float sign = (MU == 3 && c.x[3] == g.L[3] - 1) ? (float)g.t_sign : 1.0f;
+    load_link<P, RECON>(u, a.gauge_fwd[MU], idx, g.stride, sign);
+    matvec_f2<false>(uh, u, h);
+    reconstruct_f2<MU, SF>(acc, uh);
+  }
+  {
+    Coord nb = c;
+    nb.x[MU] = c.x[MU] == 0 ? g.L[MU] - 1 : c.x[MU] - 1;
+    const int ni = cb_index(g, nb);
+    load_spinor_f2<P>(s, n, in, in_norm, ni, g.stride);
+    project_f2<MU, SB>(h, s);
+    scale_f2<P>(h, n);
+    const float sign = (MU == 3 && nb.x[3] == g.L[3] - 1) ? (float)g.t_sign : 1.0f;
+    load_link<P, RECON>(u, a.gauge_bwd[MU], ni, g.stride, sign);
+    matvec_f2<true>(uh, u, h);
+    reconstruct_f2<MU, SB>(acc, uh);
+  }
+}
+
+// Grid: one dimension, right-hand-side groups fastest (block b covers sites (b / ng) * TX ... and
+// right-hand sides (b % ng) * NRB ...), so the groups that share a site range run together and
+// their link reads after the first come from L2.  MINB caps the registers (MINB resident blocks).
+template <typename P, int RECON, int MODE, bool DAG, bool REDUCE, int TX, int NRB, int MINB>
+__global__ void __launch_bounds__(TX * NRB, MINB) hop_kernel(const HopArgs a) {
   using T = typename P::real;
   const int tid = threadIdx.x;
   const int rl = tid / TX;
-  const int rhs = blockIdx.y * NRB + rl;
-  const int idx = blockIdx.x * TX + (tid % TX);
+  const int ng = (a.nrhs + NRB - 1) / NRB;
+  const int sblock = blockIdx.x / ng;
+  const int group = blockIdx.x - sblock * ng;
+  const int rhs = group * NRB + rl;
+  const int idx = sblock * TX + (tid % TX);
   const Geom& g = a.g;
   const bool active = idx < g.Vh && rhs < a.nrhs;
   double local = 0.0;
@@ -145,12 +303,24 @@ __global__ void __launch_bounds__(TX * NRB) hop_kernel(const HopArgs a) {
     const char* in = (const char*)a.in + (size_t)rhs * a.in_rhs_bytes;
     const float* in_norm = a.in_norm ? a.in_norm + (size_t)rhs * a.norm_rhs_stride : nullptr;
     cplx<T> acc[12];
+    if constexpr (std::is_same<T, float>::value) {
+      float2 accf[12];
 #pragma unroll
-    for (int k = 0; k < 12; ++k) acc[k] = {0, 0};
-    hop_dir<P, RECON, 0, DAG>(acc, a, c, idx, in, in_norm);
-    hop_dir<P, RECON, 1, DAG>(acc, a, c, idx, in, in_norm);
-    hop_dir<P, RECON, 2, DAG>(acc, a, c, idx, in, in_norm);
-    hop_dir<P, RECON, 3, DAG>(acc, a, c, idx, in, in_norm);
+      for (int k = 0; k < 12; ++k) accf[k] = make_float2(0.f, 0.f);
+      hop_dir_f2<P, RECON, 0, DAG>(accf, a, c, idx, in, in_norm);
+      hop_dir_f2<P, RECON, 1, DAG>(accf, a, c, idx, in, in_norm);
+      hop_dir_f2<P, RECON, 2, DAG>(accf, a, c, idx, in, in_norm);
+      hop_dir_f2<P, RECON, 3, DAG>(accf, a, c, idx, in, in_norm);
+#pragma unroll
+      for (int k = 0; k < 12; ++k) acc[k] = {accf[k].x, accf[k].y};
+    } else {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) acc[k] = {0, 0};
+      hop_dir<P, RECON, 0, DAG>(acc, a, c, idx, in, in_norm);
+      hop_dir<P, RECON, 1, DAG>(acc, a, c, idx, in, in_norm);
+      hop_dir<P, RECON, 2, DAG>(acc, a, c, idx, in, in_norm);
+      hop_dir<P, RECON, 3, DAG>(acc, a, c, idx, in, in_norm);
+    }
     const T coef = (T)a.a;
     cplx<T> out[12];
     if constexpr (MODE == HOP_PLAIN) {
@@ -201,8 +371,11 @@ __global__ void __launch_bounds__(TX * NRB) hop_kernel(const HopArgs a) {
     char* op = (char*)a.out + (size_t)rhs * a.out_rhs_bytes;
     store_spinor<P>(op, a.out_norm ? a.out_norm + (size_t)rhs * a.norm_rhs_stride : nullptr, idx, g.stride, out);
     if constexpr (REDUCE) {
+      // site sum in the compute precision (FP64 is slow on this part), block sums in FP64
+      T site = 0;
 #pragma unroll
-      for (int k = 0; k < 12; ++k) local += (double)out[k].re * out[k].re + (double)out[k].im * out[k].im;
+      for (int k = 0; k < 12; ++k) site = fmadd(out[k].re, out[k].re, fmadd(out[k].im, out[k].im, site));
+      local = (double)site;
     }
   }
   if constexpr (REDUCE) {
@@ -213,11 +386,11 @@ __global__ void __launch_bounds__(TX * NRB) hop_kernel(const HopArgs a) {
     if ((tid & 31) == 0) wsum[tid >> 5] = local;
     __syncthreads();
     if (tid < NRB) {
-      const int r = blockIdx.y * NRB + tid;
+      const int r = group * NRB + tid;
       double s = 0.0;
 #pragma unroll
       for (int w = 0; w < TX / 32; ++w) s += wsum[tid * (TX / 32) + w];
-      if (r < a.nrhs) a.partials[(size_t)r * a.part_stride + blockIdx.x] = s;
+      if (r < a.nrhs) a.partials[(size_t)r * a.part_stride + sblock] = s;
     }
   }
 }

@@ -1,5 +1,6 @@
 // Explicit instantiation of the hopping kernels for one storage precision (included by
-// dslash_{d,s,h}.cu with GBC_PREC, GBC_LAUNCH_NAME and GBC_RECONS defined).
+// dslash_{d,s,h}{0,1}.cu with GBC_RECON12 defined).  The launch shapes below are the candidates
+// the autotuner chooses from (TX sites x NRB right-hand sides per block, MINB resident blocks).
 #pragma once
 #include "dslash.cuh"
 
@@ -9,14 +10,20 @@ template <typename P, int RECON, int MODE, bool DAG, bool REDUCE>
 static int hop_shape(const HopArgs& a, HopShape sh, cudaStream_t s) {
   const int nbx = (a.g.Vh + sh.tx - 1) / sh.tx;
   auto go = [&](auto kern, int tx, int nrb) {
-    dim3 grid(nbx, (a.nrhs + nrb - 1) / nrb);
-    kern<<<grid, tx * nrb, 0, s>>>(a);
+    const int ng = (a.nrhs + nrb - 1) / nrb;
+    kern<<<(unsigned)(nbx * ng), tx * nrb, 0, s>>>(a);
     return nbx;
   };
-  if (sh.tx == 128 && sh.nrb == 1) return go(hop_kernel<P, RECON, MODE, DAG, REDUCE, 128, 1>, 128, 1);
-  if (sh.tx == 64 && sh.nrb == 1) return go(hop_kernel<P, RECON, MODE, DAG, REDUCE, 64, 1>, 64, 1);
-  if (sh.tx == 32 && sh.nrb == 4) return go(hop_kernel<P, RECON, MODE, DAG, REDUCE, 32, 4>, 32, 4);
-  if (sh.tx == 32 && sh.nrb == 12) return go(hop_kernel<P, RECON, MODE, DAG, REDUCE, 32, 12>, 32, 12);
+#define GBC_SHAPE(TX, NRB, MINB)                                 \
+  if (sh.tx == TX && sh.nrb == NRB && sh.minb == MINB) \
+    return go(hop_kernel<P, RECON, MODE, DAG, REDUCE, TX, NRB, MINB>, TX, NRB);
+  GBC_SHAPE(128, 1, 1)
+  GBC_SHAPE(128, 1, 6)
+  GBC_SHAPE(32, 4, 1)
+  GBC_SHAPE(32, 4, 5)
+  GBC_SHAPE(64, 2, 4)
+  GBC_SHAPE(32, 12, 2)
+#undef GBC_SHAPE
   return -1;
 }
 

@@ -55,11 +55,16 @@ struct HopArgs {
   int part_stride;
 };
 
-// Launch geometry chosen by the caller (autotuned): TX sites x NRB right-hand sides per block.
+// Launch geometry chosen by the caller (autotuned): TX sites x NRB right-hand sides per block,
+// MINB resident blocks per SM requested from the register allocator.
 struct HopShape {
   int tx;
   int nrb;
+  int minb;
 };
+// the compiled candidates (dslash_inst.cuh)
+constexpr HopShape kHopShapes[] = {{128, 1, 1}, {128, 1, 6}, {32, 4, 1}, {32, 4, 5}, {64, 2, 4}, {32, 12, 2}};
+constexpr int kNumHopShapes = 6;
 
 // Returns the number of x-blocks launched (partials per right-hand side), or -1 if the
 // (precision, recon, shape) combination is not compiled.

@@ -6,6 +6,7 @@ void precond_free(gbc_ctx* c) {
   if (!c) return;
   c->precond = nullptr;
 }
+void precond_apply(gbc_ctx* c, const Spinor& in, const Spinor& out) { blas_copy(c->g, out, in, c->stream); }
 }  // namespace gbc
 
 extern "C" int gbc_load_precond(gbc_ctx* c, const char* path) {

@@ -18,7 +18,10 @@
 #include <cmath>
 #include <cstring>
 
+#include <complex>
+
 #include "ctx.h"
+#include "krylov.h"
 
 namespace gbc {
 
@@ -104,7 +107,8 @@ CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b
   std::vector<double> rr = fetch(c, 1, n);
   std::vector<double> bb = norm2(c, b);
   std::vector<CGScalars> hs(n);
-  std::vector<double> maxrr(n);
+  std::vector<double> maxrr(n), last_rel(n, HUGE_VAL);
+  std::vector<int> stall(n, 0);
   for (int i = 0; i < n; ++i) {
     CGScalars& q = hs[i];
     std::memset(&q, 0, sizeof(q));
@@ -152,7 +156,12 @@ CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b
             q.b = q.c_prev > 0 ? nr[i] / q.c_prev : 0.0;
             q.c = q.cp = nr[i];
             maxrr[i] = std::sqrt(nr[i]);
-            if (!(nr[i] > q.rsd_sq)) {
+            // the true residual has hit the accumulator precision's floor when three reliable
+            // updates in a row fail to halve it: stop this right-hand side (the outer FP64 loop
+            // takes over from there)
+            stall[i] = nr[i] > 0.25 * last_rel[i] ? stall[i] + 1 : 0;
+            last_rel[i] = nr[i];
+            if (!(nr[i] > q.rsd_sq) || stall[i] >= 3) {
               q.active = 0;
               q.b = 0;
             }
@@ -287,6 +296,179 @@ CgStats reliable_cg(gbc_ctx* c, int po, const Spinor& psi, const Spinor& chi, do
   return st;
 }
 
+// Batched right-preconditioned FGMRES(m) on M~ x = b (FlexibleArnoldiT + Givens + LeastSquaresSolve,
+// syssolver_linop_fgmres_dr.{h:31-148, cc:77-195, 256-273, 459-765}, NDefl = 0).  Krylov vectors in
+// precision pa, operator in po; the preconditioner (learned network) maps V_j to Z_j, or Z_j = V_j.
+// Orthogonalisation: classical Gram-Schmidt applied twice (two block reductions per step instead of
+// j + 1 dependent ones).  Stops a right-hand side when |g_{j+1}| <= tol |b|.
+CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, double tol, int maxit, int m,
+               bool use_precond, const std::vector<int>& active0) {
+  using cd = std::complex<double>;
+  const int n = x.nrhs;
+  const Geom& g = c->g;
+  cudaStream_t s = c->stream;
+  if (m < 1) m = 1;
+  if (m > kMaxKrylov - 1) m = kMaxKrylov - 1;
+  VecList V, Z;
+  for (int j = 0; j <= m; ++j) V.v[j] = sub(workspace(c, 300 + j, pa, n), 0, n);
+  const bool prec = use_precond && c->precond != nullptr;
+  for (int j = 0; j < m; ++j) Z.v[j] = prec ? sub(workspace(c, 340 + j, pa, n), 0, n) : V.v[j];
+  Spinor w = sub(workspace(c, 380, pa, n), 0, n);
+  Spinor oin = sub(workspace(c, 381, po, n), 0, n);
+  Spinor oout = sub(workspace(c, 382, po, n), 0, n);
+  Spinor te = sub(workspace(c, 383, po, n), 0, n);
+  Red kred{c->d_kpartials, c->kpart_stride, c->d_kresult};
+  CgStats st;
+  st.iters.assign(n, 0);
+  st.status.assign(n, GBC_OK);
+  std::vector<double> bb = norm2(c, b);
+  std::vector<int> done(n);
+  for (int i = 0; i < n; ++i) done[i] = !active0[i];
+  auto apply_A = [&](const Spinor& in, const Spinor& out) {
+    if (po == pa) {
+      apply_meo(c, po, false, in, out, te, false);
+    } else {
+      blas_copy(g, oin, in, s);
+      apply_meo(c, po, false, oin, oout, te, false);
+      blas_copy(g, out, oout, s);
+    }
+  };
+  auto put_coef = [&](const std::vector<cd>& cf, int rows) {  // cf[row * n + rhs]
+    for (size_t k = 0; k < cf.size(); ++k) c->h_kcoef[k] = make_double2(cf[k].real(), cf[k].imag());
+    GBC_CUDA(cudaMemcpyAsync(c->d_kcoef, c->h_kcoef, sizeof(double2) * rows * n, cudaMemcpyHostToDevice, s));
+  };
+  int total = 0;
+  while (total < maxit) {
+    // r = b - A x
+    apply_A(x, w);
+    blas_xmy_norm2(g, b, w, red(c), s);
+    std::vector<double> rr = fetch(c, 1, n);
+    std::vector<double> beta(n);
+    bool all = true;
+    for (int i = 0; i < n; ++i) {
+      beta[i] = std::sqrt(rr[i]);
+      if (!std::isfinite(beta[i])) {
+        st.status[i] = GBC_ERR_NONFINITE;
+        done[i] = 1;
+      }
+      if (!done[i] && beta[i] <= tol * std::sqrt(bb[i])) done[i] = 1;
+      all &= done[i] != 0;
+    }
+    if (all) break;
+    std::vector<cd> a(n);
+    for (int i = 0; i < n; ++i) a[i] = done[i] ? 0.0 : 1.0 / beta[i];
+    put_coef(a, 1);
+    blas_cax(g, c->d_kcoef, w, V.v[0], s);
+    // per right-hand side: R (column-major, R[col][row]), g, Givens (c, s)
+    std::vector<std::vector<cd>> R(n, std::vector<cd>((m + 1) * m, 0.0)), gv(n, std::vector<cd>(m + 1, 0.0));
+    std::vector<std::vector<cd>> gc(n, std::vector<cd>(m)), gs(n, std::vector<cd>(m));
+    std::vector<int> dim(n, 0), cyc_done(done);
+    for (int i = 0; i < n; ++i) gv[i][0] = beta[i];
+    int j;
+    for (j = 0; j < m && total < maxit; ++j) {
+      if (prec) precond_apply(c, V.v[j], Z.v[j]);
+      apply_A(Z.v[j], w);
+      std::vector<cd> h((j + 1) * n, 0.0);
+      for (int pass = 0; pass < 2; ++pass) {
+        multi_cdot(g, V, j + 1, w, kred, s);
+        GBC_CUDA(cudaMemcpyAsync(c->h_kresult, c->d_kresult, sizeof(double) * 2 * (j + 1) * n, cudaMemcpyDeviceToHost, s));
+        sync(c);
+        std::vector<cd> hp((j + 1) * n);
+        for (int q = 0; q <= j; ++q)
+          for (int i = 0; i < n; ++i) {
+            cd v(c->h_kresult[(q * 2 + 0) * n + i], c->h_kresult[(q * 2 + 1) * n + i]);
+            if (cyc_done[i]) v = 0.0;
+            hp[q * n + i] = -v;
+            h[q * n + i] += v;
+          }
+        put_coef(hp, j + 1);
+        multi_caxpy(g, V, j + 1, c->d_kcoef, w, 1.0, s);
+      }
+      std::vector<double> wn2 = norm2(c, w);
+      ++total;
+      std::vector<cd> inv(n, 0.0);
+      bool all_c = true;
+      for (int i = 0; i < n; ++i) {
+        if (cyc_done[i]) continue;
+        ++st.iters[i];
+        const double wn = std::sqrt(wn2[i]);
+        std::vector<cd>& Ri = R[i];
+        for (int q = 0; q <= j; ++q) Ri[j * (m + 1) + q] = h[q * n + i];
+        Ri[j * (m + 1) + j + 1] = wn;
+        // previous rotations on the new column
+        for (int q = 0; q < j; ++q) {
+          cd A = Ri[j * (m + 1) + q], B = Ri[j * (m + 1) + q + 1];
+          Ri[j * (m + 1) + q] = std::conj(gc[i][q]) * A + std::conj(gs[i][q]) * B;
+          Ri[j * (m + 1) + q + 1] = -gs[i][q] * A + gc[i][q] * B;
+        }
+        // new rotation (Givens, syssolver_linop_fgmres_dr.h:31-148)
+        cd f = Ri[j * (m + 1) + j], gg = Ri[j * (m + 1) + j + 1], rv;
+        if (f == 0.0) {
+          gc[i][j] = 0.0;
+          gs[i][j] = 1.0;
+          rv = gg;
+        } else if (gg == 0.0) {
+          gs[i][j] = 0.0;
+          gc[i][j] = std::conj(f) / std::abs(f);
+          rv = std::abs(f);
+        } else {
+          double t = std::sqrt(std::norm(f) + std::norm(gg));
+          rv = t;
+          gc[i][j] = f / t;
+          gs[i][j] = gg / t;
+        }
+        Ri[j * (m + 1) + j] = rv;
+        Ri[j * (m + 1) + j + 1] = 0.0;
+        cd A = gv[i][j], B = gv[i][j + 1];
+        gv[i][j] = std::conj(gc[i][j]) * A + std::conj(gs[i][j]) * B;
+        gv[i][j + 1] = -gs[i][j] * A + gc[i][j] * B;
+        dim[i] = j + 1;
+        const double est = std::abs(gv[i][j + 1]);
+        if (!std::isfinite(est)) {
+          st.status[i] = GBC_ERR_NONFINITE;
+          cyc_done[i] = done[i] = 1;
+          continue;
+        }
+        // converged, or exact (happy) breakdown of the Arnoldi process
+        if (est <= tol * std::sqrt(bb[i]) || wn < 1e-14 * std::sqrt(bb[i])) cyc_done[i] = 1;
+        else inv[i] = 1.0 / wn;
+        all_c &= cyc_done[i] != 0;
+      }
+      if (j + 1 <= m) {
+        put_coef(inv, 1);
+        blas_cax(g, c->d_kcoef, w, V.v[j + 1], s);
+      }
+      bool everyone = true;
+      for (int i = 0; i < n; ++i) everyone &= cyc_done[i] != 0;
+      if (everyone) {
+        ++j;
+        break;
+      }
+    }
+    // least squares R eta = g per right-hand side, then x += Z eta
+    const int jmax = std::min(j, m);
+    std::vector<cd> eta((size_t)jmax * n, 0.0);
+    for (int i = 0; i < n; ++i) {
+      const int d = dim[i];
+      if (d == 0 || done[i]) continue;
+      std::vector<cd> e(d);
+      for (int row = d - 1; row >= 0; --row) {
+        cd v = gv[i][row];
+        for (int col = row + 1; col < d; ++col) v -= R[i][col * (m + 1) + row] * e[col];
+        e[row] = v / R[i][row * (m + 1) + row];
+      }
+      for (int q = 0; q < d; ++q) eta[q * n + i] = e[q];
+    }
+    if (jmax > 0) {
+      put_coef(eta, jmax);
+      multi_caxpy(g, Z, jmax, c->d_kcoef, x, 1.0, s);
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    if (!done[i] && st.status[i] == GBC_OK) st.status[i] = GBC_ERR_NOT_CONVERGED;
+  return st;
+}
+
 }  // namespace
 
 int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_canon, const double* chi_canon,
@@ -296,7 +478,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   if (p.max_iter <= 0) p.max_iter = 10000;
   if (!(p.delta > 0)) p.delta = 0.1;
   if (!(p.rsd_tolerance_factor > 0)) p.rsd_tolerance_factor = 10.0;
-  if (!(p.inner_tol > 0)) p.inner_tol = 1e-5;
+  if (!(p.inner_tol > 0)) p.inner_tol = 1e-6;
   if (p.inner_max_iter <= 0) p.inner_max_iter = p.max_iter;
   if (p.nkrylov <= 0) p.nkrylov = 16;
   int sloppy = p.sloppy_precision ? p.sloppy_precision : c->opts.sloppy_precision;
@@ -432,6 +614,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
       }
       std::vector<double> rr = fetch(c, 1, n);
       bool all = true;
+      double worst = 0.0;
       for (int i = 0; i < n; ++i) {
         if (done[i]) continue;
         if (!std::isfinite(rr[i])) {
@@ -440,7 +623,10 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
           continue;
         }
         if (rr[i] <= p.rsd_target * p.rsd_target * bb[i]) done[i] = 1;
-        else all = false;
+        else {
+          all = false;
+          worst = std::max(worst, std::sqrt(rr[i] / bb[i]));
+        }
       }
       if (all || it == max_outer || total >= p.max_iter) break;
       std::vector<int> active(n);
@@ -450,11 +636,21 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
       }
       // inner right-hand side in the accumulator precision
       blas_copy(g, rsl, rd, s);
-      if (!mdagm) apply_meo(c, pa, true, rsl, rhs, teh, false);
-      else blas_copy(g, rhs, rsl, s);
-      // never ask the inner solve for more than the outer target needs
-      CgCfg cfg{pa, sloppy, p.inner_tol, p.inner_max_iter, p.delta, 1};
-      CgStats st = cg_normal(c, cfg, es, rhs, true, active);
+      // never ask the inner solve for more than the outer target needs: the reduction still
+      // missing is target / worst, taken with a factor 2 of margin (but no looser than 0.1)
+      double need = 0.5 * p.rsd_target / worst;
+      double itol = std::min(0.1, std::max(p.inner_tol, need));
+      CgStats st;
+      if (p.solver == GBC_SOLVER_FGMRES && !mdagm) {
+        // flexible GMRES on M~ e = r directly (preconditioned by the learned network if loaded)
+        blas_zero(g, es, s);
+        st = fgmres(c, pa, sloppy, es, rsl, itol, p.inner_max_iter, p.nkrylov, p.use_precond != 0, active);
+      } else {
+        if (!mdagm) apply_meo(c, pa, true, rsl, rhs, teh, false);
+        else blas_copy(g, rhs, rsl, s);
+        CgCfg cfg{pa, sloppy, itol, p.inner_max_iter, p.delta, 1};
+        st = cg_normal(c, cfg, es, rhs, true, active);
+      }
       reliable += st.reliable;
       int mx = 0;
       for (int i = 0; i < n; ++i) {

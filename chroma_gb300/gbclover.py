@@ -26,7 +26,7 @@ SYS_MEO, SYS_MDAGM, SYS_FULL = range(3)
 # every entry point include/gbclover.h declares
 EXPORTS = ["gbc_create", "gbc_destroy", "gbc_strerror", "gbc_last_error", "gbc_load_gauge", "gbc_load_clover",
            "gbc_get_clover", "gbc_apply", "gbc_solve", "gbc_solve_device", "gbc_load_precond",
-           "gbc_gauge_synthetic", "gbc_time_operator"]
+           "gbc_gauge_synthetic", "gbc_time_operator", "gbc_tune_report"]
 
 
 class Geom(C.Structure):
@@ -79,6 +79,8 @@ def load(path=LIB_PATH):
     lib.gbc_strerror.argtypes = [C.c_int]
     lib.gbc_last_error.restype = C.c_char_p
     lib.gbc_last_error.argtypes = [C.c_void_p]
+    lib.gbc_tune_report.restype = C.c_char_p
+    lib.gbc_tune_report.argtypes = [C.c_void_p]
     lib.gbc_load_gauge.argtypes = [C.c_void_p, dp]
     lib.gbc_load_clover.argtypes = [C.c_void_p, dp, dp]
     lib.gbc_get_clover.argtypes = [C.c_void_p, dp, dp, dp, C.POINTER(C.c_int)]
@@ -219,6 +221,9 @@ class Context:
         self._check(self.lib.gbc_time_operator(self.h, int(op), int(prec), int(nrhs), int(iters), int(bool(flush_l2)),
                                                C.byref(sec), C.byref(byt)), "time_operator")
         return sec.value, byt.value
+
+    def tune_report(self):
+        return self.lib.gbc_tune_report(self.h).decode()
 
     def load_precond(self, path):
         self._check(self.lib.gbc_load_precond(self.h, path.encode()), "load_precond")

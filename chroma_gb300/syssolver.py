@@ -111,7 +111,7 @@ class SysSolverGB300CloverParams:
     Verbose: bool = False
     NKrylov: int = 16
     PrecondWeights: str = None
-    InnerTol: float = 1e-5
+    InnerTol: float = 1e-6
 
     @classmethod
     def from_xml(cls, xml, path="."):
@@ -136,7 +136,7 @@ class SysSolverGB300CloverParams:
         p.Verbose = node.findtext("Verbose", "false").strip().lower() == "true"
         p.NKrylov = int(node.findtext("NKrylov", "16"))
         p.PrecondWeights = node.findtext("PrecondWeights")
-        p.InnerTol = float(node.findtext("InnerTol", "1e-5"))
+        p.InnerTol = float(node.findtext("InnerTol", "1e-6"))
         return p
 
 

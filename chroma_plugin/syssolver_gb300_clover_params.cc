@@ -8,7 +8,7 @@ namespace Chroma
   SysSolverGB300CloverParams::SysSolverGB300CloverParams()
     : MaxIter(10000), RsdTarget(1.0e-10), AntiPeriodicT(true), Delta(0.1), SolverType("MIXED"),
       CudaSloppyPrecision("HALF"), CudaSloppyReconstruct("RECONS_12"), RsdToleranceFactor(10),
-      SilentFail(false), backup_invP(false), verboseP(false), NKrylov(16), InnerTol(1.0e-5), MaxRHS(12)
+      SilentFail(false), backup_invP(false), verboseP(false), NKrylov(16), InnerTol(1.0e-6), MaxRHS(12)
   {}
 
   SysSolverGB300CloverParams::SysSolverGB300CloverParams(XMLReader& xml, const std::string& path)

@@ -103,7 +103,7 @@ typedef struct gbc_solve_params {
   double delta;               /* Delta (reliable-update trigger)                    */
   double rsd_tolerance_factor;/* RsdToleranceFactor: failure threshold (default 10)  */
   int sloppy_precision;       /* 0 = context default                                */
-  double inner_tol;           /* GBC_SOLVER_MIXED inner relative tolerance (0 = 1e-5)*/
+  double inner_tol;           /* GBC_SOLVER_MIXED inner relative tolerance (0 = 1e-6)*/
   int inner_max_iter;         /* 0 = max_iter                                       */
   int nkrylov;                /* FGMRES NKrylov (0 = 16)                            */
   int use_precond;            /* FGMRES: apply the loaded learned preconditioner     */
@@ -133,6 +133,9 @@ int gbc_create(gbc_ctx** ctx, const gbc_geom* geom, const gbc_action* act, const
 void gbc_destroy(gbc_ctx* ctx);
 const char* gbc_strerror(int status);
 const char* gbc_last_error(gbc_ctx* ctx);
+/* The stencil launch shapes the autotuner picked so far, one line per kernel configuration
+   (the role of QUDA's AutotuneDslash tag; GBC_AUTOTUNE=0 in the environment disables tuning). */
+const char* gbc_tune_report(gbc_ctx* ctx);
 
 /* ---- fields ------------------------------------------------------------------------------ */
 /* Links from FermState::getLinks() (BC applied, possibly smeared); builds the clover term and
