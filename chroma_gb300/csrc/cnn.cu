@@ -1,0 +1,663 @@
+// Learned preconditioner: a gauge-covariant convolutional network approximating M~^-1.
+//
+// Fields live on the whole lattice in even-odd order (site j = parity * Vh + cb index) as
+// [site][channel][colour] complex FP32.  A layer maps C_in to C_out channels:
+//
+//     out(x)[o][a] = sum_{d=0..8} sum_i W_d[o][i] (T_d h)(x)[i][a]
+//     T_0 h(x) = h(x),  T_{+mu} h(x) = U_mu(x) h(x+mu),  T_{-mu} h(x) = U_mu(x-mu)^dag h(x-mu)
+//
+// W acts on channels only and the links on colour only, so every layer (and the network) is
+// gauge covariant.  The channel mixing is a GEMM over the rows (site, colour): the gathered
+// T_d h form a 9*C_in complex row, staged in shared memory as BF16, and mma.sync m16n8k16
+// (BF16 in, FP32 accumulate) multiplies it by the real form of W.  The network is linear; it
+// takes the odd-site input as channels = spins with zero even sites and returns its odd sites.
+//
+// Backward: the input gradient of a layer is the same layer with W'_{+mu} = W_{-mu}^H,
+// W'_{-mu} = W_{+mu}^H, W'_0 = W_0^H (T_{+mu}^dag = T_{-mu}), and the weight gradient is
+// sum over rows of delta_out (x) conj(gathered input), also on the tensor cores.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "cnn.h"
+#include "ctx.h"
+#include "gbc_device.cuh"
+
+namespace gbc {
+namespace {
+
+constexpr int CT = 128;     // threads per block
+constexpr int SITES = 32;   // sites per block -> 96 rows (site, colour)
+constexpr int ROWS = SITES * 3;
+
+__host__ __device__ constexpr int kpad(int cin) { return ((9 * cin * 2 + 15) / 16) * 16; }
+__host__ __device__ constexpr int npad(int cout) { return ((2 * cout + 7) / 8) * 8; }
+
+__device__ __forceinline__ Coord eo_coords(const Geom& g, int j) {
+  const int par = j >= g.Vh ? 1 : 0;
+  return cb_coords(g, j - par * g.Vh, par);
+}
+__device__ __forceinline__ int eo_index(const Geom& g, const Coord& c) {
+  const int par = (c.x[0] + c.x[1] + c.x[2] + c.x[3]) & 1;
+  return par * g.Vh + cb_index(g, c);
+}
+
+// neighbour site and link (row-major 3x3, already daggered for backward hops) of direction d
+__device__ __forceinline__ int hop_site(const Geom& g, const float2* links, int j, int d, float2 (&u)[9]) {
+  Coord c = eo_coords(g, j);
+  const int mu = (d - 1) >> 1;
+  const bool bwd = ((d - 1) & 1) != 0;
+  if (!bwd) {
+    const float2* L = links + ((size_t)j * 4 + mu) * 9;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) u[k] = L[k];
+    c.x[mu] = c.x[mu] + 1 == g.L[mu] ? 0 : c.x[mu] + 1;
+    return eo_index(g, c);
+  }
+  c.x[mu] = c.x[mu] == 0 ? g.L[mu] - 1 : c.x[mu] - 1;
+  const int n = eo_index(g, c);
+  const float2* L = links + ((size_t)n * 4 + mu) * 9;
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float2 e = L[3 * k + r];
+      u[3 * r + k] = make_float2(e.x, -e.y);
+    }
+  return n;
+}
+
+// G[row = s*3 + a][k = (d*CIN + i)*2 + re/im] = (T_d h)(site)[i][a] in BF16; pad columns zeroed
+template <int CIN>
+__device__ void gather_tile(__nv_bfloat16* G, const Geom& g, int V, const float2* links, const float2* h, int site0) {
+  constexpr int KP = kpad(CIN);
+  for (int p = threadIdx.x; p < SITES * 9; p += blockDim.x) {
+    const int s = p % SITES, d = p / SITES;
+    const int j = site0 + s;
+    __nv_bfloat16* row0 = G + (size_t)(s * 3) * KP + d * CIN * 2;
+    if (j >= V) {
+      for (int a = 0; a < 3; ++a)
+        for (int k = 0; k < CIN * 2; ++k) row0[a * KP + k] = __float2bfloat16(0.f);
+      continue;
+    }
+    if (d == 0) {
+      const float2* src = h + (size_t)j * CIN * 3;
+      for (int i = 0; i < CIN; ++i)
+        for (int a = 0; a < 3; ++a) {
+          const float2 v = src[i * 3 + a];
+          row0[a * KP + 2 * i] = __float2bfloat16(v.x);
+          row0[a * KP + 2 * i + 1] = __float2bfloat16(v.y);
+        }
+      continue;
+    }
+    float2 u[9];
+    const int n = hop_site(g, links, j, d, u);
+    const float2* src = h + (size_t)n * CIN * 3;
+    for (int i = 0; i < CIN; ++i) {
+      const float2 x0 = src[i * 3], x1 = src[i * 3 + 1], x2 = src[i * 3 + 2];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float2 u0 = u[3 * a], u1 = u[3 * a + 1], u2 = u[3 * a + 2];
+        const float re = u0.x * x0.x - u0.y * x0.y + u1.x * x1.x - u1.y * x1.y + u2.x * x2.x - u2.y * x2.y;
+        const float im = u0.x * x0.y + u0.y * x0.x + u1.x * x1.y + u1.y * x1.x + u2.x * x2.y + u2.y * x2.x;
+        row0[a * KP + 2 * i] = __float2bfloat16(re);
+        row0[a * KP + 2 * i + 1] = __float2bfloat16(im);
+      }
+    }
+  }
+  // zero the K padding
+  constexpr int K = 9 * CIN * 2;
+  if (KP > K)
+    for (int p = threadIdx.x; p < ROWS * (KP - K); p += blockDim.x) {
+      const int r = p / (KP - K), k = K + p % (KP - K);
+      G[(size_t)r * KP + k] = __float2bfloat16(0.f);
+    }
+}
+
+__device__ __forceinline__ uint32_t ld_bf16x2(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// out[b][j][o][a] = (G W^T)[row][2o + re/im]
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, const float2* links, const float2* hin,
+                                                   float2* hout, const __nv_bfloat16* Wr) {
+  constexpr int KP = kpad(CIN), NP = npad(COUT);
+  extern __shared__ __align__(16) unsigned char smem[];
+  __nv_bfloat16* G = reinterpret_cast<__nv_bfloat16*>(smem);
+  __nv_bfloat16* W = G + ROWS * KP;
+  const int b = blockIdx.y;
+  const int site0 = blockIdx.x * SITES;
+  const float2* h = hin + (size_t)b * V * CIN * 3;
+  for (int p = threadIdx.x; p < NP * KP; p += blockDim.x) W[p] = Wr[p];
+  gather_tile<CIN>(G, g, V, links, h, site0);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  constexpr int MT = ROWS / 16, NT = NP / 8;
+  float2* out = hout + (size_t)b * V * COUT * 3;
+  for (int t = warp; t < MT * NT; t += CT / 32) {
+    const int mt = t % MT, nt = t / MT;
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int ks = 0; ks < KP / 16; ++ks) {
+      const __nv_bfloat16* A0 = G + (size_t)(mt * 16 + gid) * KP + ks * 16 + 2 * tig;
+      const __nv_bfloat16* A1 = A0 + 8 * KP;
+      uint32_t a[4] = {ld_bf16x2(A0), ld_bf16x2(A1), ld_bf16x2(A0 + 8), ld_bf16x2(A1 + 8)};
+      const __nv_bfloat16* B0 = W + (size_t)(nt * 8 + gid) * KP + ks * 16 + 2 * tig;
+      uint32_t bb[2] = {ld_bf16x2(B0), ld_bf16x2(B0 + 8)};
+      mma_bf16(c, a, bb);
+    }
+    const int o = nt * 4 + tig;
+    if (o < COUT) {
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int row = mt * 16 + gid + 8 * half;
+        const int s = row / 3, a = row % 3;
+        const int j = site0 + s;
+        if (j < V) out[((size_t)j * COUT + o) * 3 + a] = make_float2(c[2 * half], c[2 * half + 1]);
+      }
+    }
+  }
+}
+
+// gradient of the real-form weights: dW[n][k] += sum_rows delta[row][n] * G[row][k]
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(CT) wgrad_kernel(Geom g, int V, const float2* links, const float2* hin,
+                                                   const float2* delta, float* dW) {
+  constexpr int KP = kpad(CIN), NP = npad(COUT), MP = ((NP + 15) / 16) * 16;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __nv_bfloat16* G = reinterpret_cast<__nv_bfloat16*>(smem);
+  __nv_bfloat16* Dt = G + ROWS * KP;  // [MP][ROWS]: delta transposed (A operand, row-major M x K)
+  const int b = blockIdx.y;
+  const int site0 = blockIdx.x * SITES;
+  gather_tile<CIN>(G, g, V, links, hin + (size_t)b * V * CIN * 3, site0);
+  const float2* dl = delta + (size_t)b * V * COUT * 3;
+  for (int p = threadIdx.x; p < MP * ROWS; p += blockDim.x) {
+    const int n = p / ROWS, row = p % ROWS;
+    const int s = row / 3, a = row % 3, j = site0 + s, o = n >> 1;
+    float v = 0.f;
+    if (n < 2 * COUT && j < V) {
+      const float2 d = dl[((size_t)j * COUT + o) * 3 + a];
+      v = (n & 1) ? d.y : d.x;
+    }
+    Dt[(size_t)n * ROWS + row] = __float2bfloat16(v);
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gid = lane >> 2, tig = lane & 3;
+  constexpr int MT = MP / 16, NT = KP / 8;
+  for (int t = warp; t < MT * NT; t += CT / 32) {
+    const int mt = t % MT, nt = t / MT;
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int ks = 0; ks < ROWS / 16; ++ks) {
+      const __nv_bfloat16* A0 = Dt + (size_t)(mt * 16 + gid) * ROWS + ks * 16 + 2 * tig;
+      const __nv_bfloat16* A1 = A0 + 8 * ROWS;
+      uint32_t a[4] = {ld_bf16x2(A0), ld_bf16x2(A1), ld_bf16x2(A0 + 8), ld_bf16x2(A1 + 8)};
+      // B (K = rows x N = k columns), col-major fragment: (k = 2 tig + {0,1}, n = gid)
+      const int col = nt * 8 + gid;
+      const int r0 = ks * 16 + 2 * tig;
+      uint32_t bb[2] = {pack_bf16(G[(size_t)r0 * KP + col], G[(size_t)(r0 + 1) * KP + col]),
+                        pack_bf16(G[(size_t)(r0 + 8) * KP + col], G[(size_t)(r0 + 9) * KP + col])};
+      mma_bf16(c, a, bb);
+    }
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int n = mt * 16 + gid + 8 * half;
+      const int k = nt * 8 + 2 * tig;
+      if (n < 2 * COUT) {
+        atomicAdd(&dW[(size_t)n * KP + k], c[2 * half]);
+        atomicAdd(&dW[(size_t)n * KP + k + 1], c[2 * half + 1]);
+      }
+    }
+  }
+}
+
+// odd-site spinor field (precision P) -> layer-0 activations (even sites zero)
+template <typename P>
+__global__ void embed_kernel(Geom g, int V, Spinor f, float2* act) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (j >= V) return;
+  float2* out = act + ((size_t)b * V + j) * 12;
+  if (j < g.Vh) {
+    for (int k = 0; k < 12; ++k) out[k] = make_float2(0.f, 0.f);
+    return;
+  }
+  cplx<typename P::real> v[12];
+  load_spinor<P>(v, (const char*)f.v + (size_t)b * f.rhs_bytes, f.norm ? f.norm + (size_t)b * f.norm_rhs_stride : nullptr,
+                 j - g.Vh, f.stride);
+  for (int k = 0; k < 12; ++k) out[k] = make_float2((float)v[k].re, (float)v[k].im);
+}
+
+template <typename P>
+__global__ void extract_kernel(Geom g, int V, const float2* act, Spinor f) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (i >= g.Vh) return;
+  const float2* src = act + ((size_t)b * V + g.Vh + i) * 12;
+  cplx<typename P::real> v[12];
+  for (int k = 0; k < 12; ++k) v[k] = {(typename P::real)src[k].x, (typename P::real)src[k].y};
+  store_spinor<P>((char*)f.v + (size_t)b * f.rhs_bytes, f.norm ? f.norm + (size_t)b * f.norm_rhs_stride : nullptr, i,
+                  f.stride, v);
+}
+
+// canonical complex128 [V][12] (rhs b at offset b*V*12) -> activations, odd sites only
+__global__ void embed_canon_kernel(Geom g, int V, const double2* canon, float2* act) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (j >= V) return;
+  float2* out = act + ((size_t)b * V + j) * 12;
+  if (j < g.Vh) {
+    for (int k = 0; k < 12; ++k) out[k] = make_float2(0.f, 0.f);
+    return;
+  }
+  const Coord c = eo_coords(g, j);
+  const double2* src = canon + ((size_t)b * V + full_index(g, c)) * 12;
+  for (int k = 0; k < 12; ++k) out[k] = make_float2((float)src[k].x, (float)src[k].y);
+}
+
+__global__ void extract_canon_kernel(Geom g, int V, const float2* act, double2* canon) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (j >= V) return;
+  const Coord c = eo_coords(g, j);
+  double2* dst = canon + ((size_t)b * V + full_index(g, c)) * 12;
+  const float2* src = act + ((size_t)b * V + j) * 12;
+  for (int k = 0; k < 12; ++k)
+    dst[k] = j < g.Vh ? make_double2(0.0, 0.0) : make_double2((double)src[k].x, (double)src[k].y);
+}
+
+// loss = sum_b sum_odd |y - e|^2 / |e|^2 ; delta = 2 (y - e) / |e|^2 on odd sites, 0 elsewhere
+__global__ void loss_kernel(Geom g, int V, const float2* y, const float2* e, const double* enorm2, float2* delta,
+                            double* partial) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  double l = 0.0;
+  if (j < V) {
+    const size_t o = ((size_t)b * V + j) * 12;
+    const float inv = (float)(1.0 / enorm2[b]);
+    for (int k = 0; k < 12; ++k) {
+      float2 d = make_float2(0.f, 0.f);
+      if (j >= g.Vh) {
+        d = make_float2(y[o + k].x - e[o + k].x, y[o + k].y - e[o + k].y);
+        l += (double)(d.x * d.x + d.y * d.y) * inv;
+        d = make_float2(2.f * d.x * inv, 2.f * d.y * inv);
+      }
+      delta[o + k] = d;
+    }
+  }
+  __shared__ double sh[256];
+  sh[threadIdx.x] = l;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(partial, sh[0]);
+}
+
+__global__ void links_kernel(Geom g, int V, const double2* canon, float2* links) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= V) return;
+  const Coord c = eo_coords(g, j);
+  const long s = full_index(g, c);
+  for (int m = 0; m < 4; ++m)
+    for (int k = 0; k < 9; ++k) {
+      const double2 v = canon[(s * 4 + m) * 9 + k];
+      links[((size_t)j * 4 + m) * 9 + k] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+template <int CIN, int COUT>
+void launch_layer(const Geom& g, int V, int batch, const float2* links, const float2* in, float2* out,
+                  const __nv_bfloat16* W, cudaStream_t s) {
+  const size_t smem = (size_t)(ROWS * kpad(CIN) + npad(COUT) * kpad(CIN)) * 2;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(layer_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  dim3 grid((V + SITES - 1) / SITES, batch);
+  layer_kernel<CIN, COUT><<<grid, CT, smem, s>>>(g, V, links, in, out, W);
+  count_launch();
+}
+
+template <int CIN, int COUT>
+void launch_wgrad(const Geom& g, int V, int batch, const float2* links, const float2* in, const float2* delta,
+                  float* dW, cudaStream_t s) {
+  constexpr int MP = ((npad(COUT) + 15) / 16) * 16;
+  const size_t smem = (size_t)(ROWS * kpad(CIN) + MP * ROWS) * 2;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(wgrad_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  dim3 grid((V + SITES - 1) / SITES, batch);
+  wgrad_kernel<CIN, COUT><<<grid, CT, smem, s>>>(g, V, links, in, delta, dW);
+  count_launch();
+}
+
+void layer(const Geom& g, int V, int batch, int cin, int cout, const float2* links, const float2* in, float2* out,
+           const __nv_bfloat16* W, cudaStream_t s) {
+  if (cin == 4 && cout == 12) launch_layer<4, 12>(g, V, batch, links, in, out, W, s);
+  else if (cin == 12 && cout == 12) launch_layer<12, 12>(g, V, batch, links, in, out, W, s);
+  else if (cin == 12 && cout == 4) launch_layer<12, 4>(g, V, batch, links, in, out, W, s);
+  else if (cin == 4 && cout == 4) launch_layer<4, 4>(g, V, batch, links, in, out, W, s);
+  else throw std::string("network layer shape not compiled");
+}
+
+void wgrad(const Geom& g, int V, int batch, int cin, int cout, const float2* links, const float2* in,
+           const float2* delta, float* dW, cudaStream_t s) {
+  if (cin == 4 && cout == 12) launch_wgrad<4, 12>(g, V, batch, links, in, delta, dW, s);
+  else if (cin == 12 && cout == 12) launch_wgrad<12, 12>(g, V, batch, links, in, delta, dW, s);
+  else if (cin == 12 && cout == 4) launch_wgrad<12, 4>(g, V, batch, links, in, delta, dW, s);
+  else if (cin == 4 && cout == 4) launch_wgrad<4, 4>(g, V, batch, links, in, delta, dW, s);
+  else throw std::string("network layer shape not compiled");
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// host model
+// ---------------------------------------------------------------------------------------------
+using cf = std::complex<float>;
+
+int Cnn::cin(int l) const { return l == 0 ? 4 : hidden; }
+int Cnn::cout(int l) const { return l == nlayers - 1 ? 4 : hidden; }
+
+void Cnn::init(int hidden_, int layers_, unsigned long long seed) {
+  hidden = hidden_;
+  nlayers = layers_;
+  W.assign(nlayers, {});
+  std::mt19937_64 rng(seed);
+  std::normal_distribution<float> nd(0.f, 1.f);
+  for (int l = 0; l < nlayers; ++l) {
+    const int ci = cin(l), co = cout(l);
+    W[l].assign((size_t)9 * co * ci, cf(0, 0));
+    // start near the identity map through the self term, with small random hops (scaled so a
+    // layer roughly preserves norms)
+    const float sc = 0.1f / std::sqrt((float)(9 * ci));
+    for (auto& w : W[l]) w = cf(sc * nd(rng), sc * nd(rng));
+    for (int o = 0; o < co; ++o)
+      for (int i = 0; i < ci; ++i)
+        if (o % ci == i || (ci > co && i % co == o)) W[l][(size_t)o * ci + i] += cf(ci > co ? 1.0f / (ci / co) : 1.0f, 0);
+  }
+  m1.assign(nlayers, {});
+  m2.assign(nlayers, {});
+  for (int l = 0; l < nlayers; ++l) {
+    m1[l].assign(W[l].size() * 2, 0.f);
+    m2[l].assign(W[l].size() * 2, 0.f);
+  }
+  step = 0;
+  dirty = true;
+}
+
+static void real_form(const std::vector<cf>& Wc, int ci, int co, bool adjoint, std::vector<__nv_bfloat16>& out) {
+  // forward: rows 2*COUT (re/im of output o), K = (d*CIN + i)*2 + re/im
+  // adjoint: out channels = ci, in channels = co, W'_d = (W_{swap d})^H
+  const int oc = adjoint ? ci : co, ic = adjoint ? co : ci;
+  const int KP = kpad(ic), NP = npad(oc);
+  out.assign((size_t)NP * KP, __float2bfloat16(0.f));
+  for (int d = 0; d < 9; ++d) {
+    const int ds = adjoint ? (d == 0 ? 0 : (((d - 1) ^ 1) + 1)) : d;
+    for (int o = 0; o < oc; ++o)
+      for (int i = 0; i < ic; ++i) {
+        cf w = adjoint ? std::conj(Wc[((size_t)ds * co + i) * ci + o]) : Wc[((size_t)d * co + o) * ci + i];
+        const int k = (d * ic + i) * 2;
+        out[(size_t)(2 * o) * KP + k] = __float2bfloat16(w.real());
+        out[(size_t)(2 * o) * KP + k + 1] = __float2bfloat16(-w.imag());
+        out[(size_t)(2 * o + 1) * KP + k] = __float2bfloat16(w.imag());
+        out[(size_t)(2 * o + 1) * KP + k + 1] = __float2bfloat16(w.real());
+      }
+  }
+}
+
+void Cnn::upload(cudaStream_t s) {
+  if (!dirty) return;
+  for (int l = 0; l < nlayers; ++l) {
+    std::vector<__nv_bfloat16> a, b;
+    real_form(W[l], cin(l), cout(l), false, a);
+    real_form(W[l], cin(l), cout(l), true, b);
+    if (!dW[l]) {
+      GBC_CUDA(cudaMalloc(&dW[l], a.size() * 2));
+      GBC_CUDA(cudaMalloc(&dWadj[l], b.size() * 2));
+      GBC_CUDA(cudaMalloc(&dG[l], sizeof(float) * (size_t)npad(cout(l)) * kpad(cin(l))));
+    }
+    GBC_CUDA(cudaMemcpyAsync(dW[l], a.data(), a.size() * 2, cudaMemcpyHostToDevice, s));
+    GBC_CUDA(cudaMemcpyAsync(dWadj[l], b.data(), b.size() * 2, cudaMemcpyHostToDevice, s));
+  }
+  GBC_CUDA(cudaStreamSynchronize(s));
+  dirty = false;
+}
+
+void Cnn::release() {
+  for (int l = 0; l < 8; ++l) {
+    if (dW[l]) cudaFree(dW[l]);
+    if (dWadj[l]) cudaFree(dWadj[l]);
+    if (dG[l]) cudaFree(dG[l]);
+    dW[l] = dWadj[l] = nullptr;
+    dG[l] = nullptr;
+  }
+  for (auto& p : act) if (p) cudaFree(p);
+  act.clear();
+  if (links) cudaFree(links);
+  links = nullptr;
+  if (delta[0]) cudaFree(delta[0]);
+  if (delta[1]) cudaFree(delta[1]);
+  delta[0] = delta[1] = nullptr;
+  act_batch = 0;
+}
+
+void Cnn::ensure(gbc_ctx* c, int batch) {
+  const int V = (int)c->V;
+  if (!links || links_version != c->gauge_version) {
+    if (!links) GBC_CUDA(cudaMalloc(&links, sizeof(float2) * (size_t)V * 36));
+    links_kernel<<<(V + 127) / 128, 128, 0, c->stream>>>(c->g, V, reinterpret_cast<const double2*>(c->d_links), links);
+    count_launch();
+    links_version = c->gauge_version;
+  }
+  if (act_batch < batch) {
+    for (auto& p : act) if (p) cudaFree(p);
+    act.assign(nlayers + 1, nullptr);
+    for (int l = 0; l <= nlayers; ++l) {
+      const int ch = l == 0 ? 4 : cout(l - 1);
+      GBC_CUDA(cudaMalloc(&act[l], sizeof(float2) * (size_t)batch * V * std::max(ch, 12) * 3));
+    }
+    for (int q = 0; q < 2; ++q) {
+      if (delta[q]) cudaFree(delta[q]);
+      GBC_CUDA(cudaMalloc(&delta[q], sizeof(float2) * (size_t)batch * V * std::max(hidden, 4) * 3));
+    }
+    act_batch = batch;
+  }
+  upload(c->stream);
+}
+
+void Cnn::forward(gbc_ctx* c, int batch) {
+  const int V = (int)c->V;
+  for (int l = 0; l < nlayers; ++l) layer(c->g, V, batch, cin(l), cout(l), links, act[l], act[l + 1], dW[l], c->stream);
+}
+
+double Cnn::loss_and_grad(gbc_ctx* c, int batch, const float2* target, const double* enorm2) {
+  const int V = (int)c->V;
+  cudaStream_t s = c->stream;
+  forward(c, batch);
+  double* dl = nullptr;
+  GBC_CUDA(cudaMalloc(&dl, sizeof(double)));
+  GBC_CUDA(cudaMemsetAsync(dl, 0, sizeof(double), s));
+  dim3 grid((V + 255) / 256, batch);
+  loss_kernel<<<grid, 256, 0, s>>>(c->g, V, act[nlayers], target, enorm2, delta[0], dl);
+  count_launch();
+  for (int l = 0; l < nlayers; ++l)
+    GBC_CUDA(cudaMemsetAsync(dG[l], 0, sizeof(float) * (size_t)npad(cout(l)) * kpad(cin(l)), s));
+  int cur = 0;
+  for (int l = nlayers - 1; l >= 0; --l) {
+    wgrad(c->g, V, batch, cin(l), cout(l), links, act[l], delta[cur], dG[l], s);
+    if (l > 0) {
+      layer(c->g, V, batch, cout(l), cin(l), links, delta[cur], delta[1 - cur], dWadj[l], s);
+      cur = 1 - cur;
+    }
+  }
+  double loss = 0;
+  GBC_CUDA(cudaMemcpyAsync(&loss, dl, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GBC_CUDA(cudaStreamSynchronize(s));
+  cudaFree(dl);
+  return loss;
+}
+
+// complex gradient dL/dRe W + i dL/dIm W from the real-form gradient
+void Cnn::download_grad(cudaStream_t s, std::vector<std::vector<cf>>& grad) {
+  grad.assign(nlayers, {});
+  for (int l = 0; l < nlayers; ++l) {
+    const int ci = cin(l), co = cout(l), KP = kpad(ci);
+    std::vector<float> gr((size_t)npad(co) * KP);
+    GBC_CUDA(cudaMemcpyAsync(gr.data(), dG[l], gr.size() * 4, cudaMemcpyDeviceToHost, s));
+    GBC_CUDA(cudaStreamSynchronize(s));
+    grad[l].assign((size_t)9 * co * ci, cf(0, 0));
+    for (int d = 0; d < 9; ++d)
+      for (int o = 0; o < co; ++o)
+        for (int i = 0; i < ci; ++i) {
+          const int k = (d * ci + i) * 2;
+          const float dre = gr[(size_t)(2 * o) * KP + k] + gr[(size_t)(2 * o + 1) * KP + k + 1];
+          const float dim = gr[(size_t)(2 * o + 1) * KP + k] - gr[(size_t)(2 * o) * KP + k + 1];
+          grad[l][((size_t)d * co + o) * ci + i] = cf(dre, dim);
+        }
+  }
+}
+
+void Cnn::adam(const std::vector<std::vector<cf>>& grad, double lr) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  ++step;
+  const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
+  for (int l = 0; l < nlayers; ++l)
+    for (size_t q = 0; q < W[l].size(); ++q) {
+      const float gq[2] = {grad[l][q].real(), grad[l][q].imag()};
+      float wq[2] = {W[l][q].real(), W[l][q].imag()};
+      for (int r = 0; r < 2; ++r) {
+        float& m = m1[l][2 * q + r];
+        float& v = m2[l][2 * q + r];
+        m = b1 * m + (1 - b1) * gq[r];
+        v = b2 * v + (1 - b2) * gq[r] * gq[r];
+        wq[r] -= (float)lr * (m / c1) / (std::sqrt(v / c2) + eps);
+      }
+      W[l][q] = cf(wq[0], wq[1]);
+    }
+  dirty = true;
+}
+
+// file: "GBCW" u32 version=1, u32 layers, u32 hidden, then per layer u32 cin, u32 cout,
+// 9*cout*cin complex float32, then u64 FNV-1a of everything before it
+static uint64_t fnv1a(const unsigned char* p, size_t n) {
+  uint64_t h = 1469598103934665603ULL;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ULL;
+  }
+  return h;
+}
+
+bool Cnn::save(const std::string& path) const {
+  std::vector<unsigned char> buf;
+  auto put = [&](const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    buf.insert(buf.end(), c, c + n);
+  };
+  const char magic[4] = {'G', 'B', 'C', 'W'};
+  const uint32_t ver = 1, L = nlayers, H = hidden;
+  put(magic, 4);
+  put(&ver, 4);
+  put(&L, 4);
+  put(&H, 4);
+  for (int l = 0; l < nlayers; ++l) {
+    const uint32_t ci = cin(l), co = cout(l);
+    put(&ci, 4);
+    put(&co, 4);
+    put(W[l].data(), W[l].size() * sizeof(cf));
+  }
+  const uint64_t h = fnv1a(buf.data(), buf.size());
+  put(&h, 8);
+  std::ofstream f(path, std::ios::binary);
+  if (!f) return false;
+  f.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)buf.size());
+  return (bool)f;
+}
+
+int Cnn::load(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return GBC_ERR_PRECOND;
+  std::vector<unsigned char> buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  if (buf.size() < 16 + 8 || std::memcmp(buf.data(), "GBCW", 4) != 0) return GBC_ERR_PRECOND;
+  uint64_t h;
+  std::memcpy(&h, buf.data() + buf.size() - 8, 8);
+  if (fnv1a(buf.data(), buf.size() - 8) != h) return GBC_ERR_PRECOND;
+  uint32_t ver, L, H;
+  std::memcpy(&ver, buf.data() + 4, 4);
+  std::memcpy(&L, buf.data() + 8, 4);
+  std::memcpy(&H, buf.data() + 12, 4);
+  if (ver != 1 || L < 1 || L > 8 || (H != 4 && H != 12)) return GBC_ERR_PRECOND;
+  init((int)H, (int)L, 0);
+  size_t off = 16;
+  for (int l = 0; l < nlayers; ++l) {
+    uint32_t ci, co;
+    if (off + 8 > buf.size() - 8) return GBC_ERR_PRECOND;
+    std::memcpy(&ci, buf.data() + off, 4);
+    std::memcpy(&co, buf.data() + off + 4, 4);
+    off += 8;
+    if ((int)ci != cin(l) || (int)co != cout(l)) return GBC_ERR_PRECOND;
+    const size_t n = W[l].size() * sizeof(cf);
+    if (off + n > buf.size() - 8) return GBC_ERR_PRECOND;
+    std::memcpy(W[l].data(), buf.data() + off, n);
+    off += n;
+  }
+  if (off != buf.size() - 8) return GBC_ERR_PRECOND;
+  dirty = true;
+  return GBC_OK;
+}
+
+void cnn_apply_spinor(gbc_ctx* c, Cnn& net, const Spinor& in, const Spinor& out) {
+  const int V = (int)c->V;
+  net.ensure(c, in.nrhs);
+  dim3 grid((V + 127) / 128, in.nrhs);
+  if (in.prec == PREC_DOUBLE) embed_kernel<PrecD><<<grid, 128, 0, c->stream>>>(c->g, V, in, net.act[0]);
+  else if (in.prec == PREC_SINGLE) embed_kernel<PrecS><<<grid, 128, 0, c->stream>>>(c->g, V, in, net.act[0]);
+  else embed_kernel<PrecH><<<grid, 128, 0, c->stream>>>(c->g, V, in, net.act[0]);
+  count_launch();
+  net.forward(c, in.nrhs);
+  dim3 g2((c->g.Vh + 127) / 128, in.nrhs);
+  if (out.prec == PREC_DOUBLE) extract_kernel<PrecD><<<g2, 128, 0, c->stream>>>(c->g, V, net.act[net.nlayers], out);
+  else if (out.prec == PREC_SINGLE) extract_kernel<PrecS><<<g2, 128, 0, c->stream>>>(c->g, V, net.act[net.nlayers], out);
+  else extract_kernel<PrecH><<<g2, 128, 0, c->stream>>>(c->g, V, net.act[net.nlayers], out);
+  count_launch();
+}
+
+void cnn_embed_canon(gbc_ctx* c, Cnn& net, int batch, const double* canon_dev, float2* act) {
+  const int V = (int)c->V;
+  dim3 grid((V + 127) / 128, batch);
+  embed_canon_kernel<<<grid, 128, 0, c->stream>>>(c->g, V, reinterpret_cast<const double2*>(canon_dev), act);
+  count_launch();
+}
+
+void cnn_extract_canon(gbc_ctx* c, Cnn& net, int batch, const float2* act, double* canon_dev) {
+  const int V = (int)c->V;
+  dim3 grid((V + 127) / 128, batch);
+  extract_canon_kernel<<<grid, 128, 0, c->stream>>>(c->g, V, act, reinterpret_cast<double2*>(canon_dev));
+  count_launch();
+}
+
+}  // namespace gbc

@@ -179,6 +179,10 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce
       const HopShape sh = kHopShapes[si];
       if (sh.nrb > 1 && sh.nrb > h.nrhs) continue;  // a block would be mostly idle
       if (hop_launch(prec, recon, mode, dag, reduce, h, sh, c->stream) < 0) continue;
+      if (cudaPeekAtLastError() != cudaSuccess) {
+        cudaGetLastError();  // e.g. too many resources for this shape: not a candidate
+        continue;
+      }
       GBC_CUDA(cudaEventRecord(e0, c->stream));
       for (int k = 0; k < 3; ++k) hop_launch(prec, recon, mode, dag, reduce, h, sh, c->stream);
       GBC_CUDA(cudaEventRecord(e1, c->stream));
@@ -421,6 +425,7 @@ int gbc_load_gauge(gbc_ctx* c, const double* links) {
     }
     c->logdet_even = s;
     c->nneg = n;
+    ++c->gauge_version;
     if (n && c->opts.verbose) fprintf(stderr, "gbclover: WARNING %d negative clover eigenvalues\n", n);
     return rebuild_from_clover(c);
   });

@@ -44,6 +44,7 @@ struct gbc_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   bool have_gauge = false;
+  long gauge_version = 0;  // bumped by every gbc_load_gauge
   double link_coeff[4] = {1, 1, 1, 1};
 
   // canonical FP64 copies on the device

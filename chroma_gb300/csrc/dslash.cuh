@@ -282,6 +282,92 @@ __device__ __forceinline__ void hop_dir_f2(float2 (&acc)[12], const HopArgs& a, 
   }
 }
 
+// ---- links shared by the right-hand sides of a block (NRB > 1) ----------------------------------
+// Each (site, direction) link is loaded and reconstructed once per block and kept in shared memory
+// as the pairs (ur, ur, -ui, ui) that the packed complex multiply consumes; without this every
+// right-hand side would redo the 12-real reconstruction.  Layout [dir][element][site] keeps a
+// warp's 32 sites on consecutive 16-byte words.
+template <typename P, int RECON, int TX>
+__device__ __forceinline__ void stage_links(float4 (*lsm)[9][TX], const HopArgs& a, int sblock) {
+  const Geom& g = a.g;
+  for (int p = threadIdx.x; p < 8 * TX; p += blockDim.x) {
+    const int s = p % TX, d = p / TX;
+    const int idx = sblock * TX + s;
+    if (idx >= g.Vh) continue;
+    const int mu = d >> 1;
+    const bool bwd = d & 1;
+    const Coord c = cb_coords(g, idx, a.out_parity);
+    cplx<float> u[9];
+    if (!bwd) {
+      const float sign = (mu == 3 && c.x[3] == g.L[3] - 1) ? (float)g.t_sign : 1.0f;
+      load_link<P, RECON>(u, a.gauge_fwd[mu], idx, g.stride, sign);
+    } else {
+      Coord n = c;
+      n.x[mu] = c.x[mu] == 0 ? g.L[mu] - 1 : c.x[mu] - 1;
+      const float sign = (mu == 3 && n.x[3] == g.L[3] - 1) ? (float)g.t_sign : 1.0f;
+      load_link<P, RECON>(u, a.gauge_bwd[mu], cb_index(g, n), g.stride, sign);
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        // element multiplying h[k] in row r: U[r][k] (forward) or conj(U[k][r]) (backward)
+        const cplx<float> e = bwd ? conj(u[3 * k + r]) : u[3 * r + k];
+        lsm[d][3 * r + k][s] = make_float4(e.re, e.re, -e.im, e.im);
+      }
+  }
+}
+
+template <int TX>
+__device__ __forceinline__ void matvec_sm(float2 (&uh)[2][3], const float4 (*lsm)[9][TX], int d, int s,
+                                          const float2 (&h)[2][3]) {
+  float2 hs[2][3];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) hs[q][c] = make_float2(h[q][c].y, h[q][c].x);
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float4 ab = lsm[d][3 * r + k][s];
+      const float2 A = make_float2(ab.x, ab.y), B = make_float2(ab.z, ab.w);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        float2 v = k == 0 ? __fmul2_rn(A, h[q][0]) : __ffma2_rn(A, h[q][k], uh[q][r]);
+        uh[q][r] = __ffma2_rn(B, hs[q][k], v);
+      }
+    }
+}
+
+template <typename P, int MU, bool DAG, int TX>
+__device__ __forceinline__ void hop_dir_sm(float2 (&acc)[12], const float4 (*lsm)[9][TX], int s, const HopArgs& a,
+                                           const Coord& c, const char* in, const float* in_norm) {
+  constexpr int SF = DAG ? +1 : -1;
+  constexpr int SB = DAG ? -1 : +1;
+  const Geom& g = a.g;
+  float2 sp[12], h[2][3], uh[2][3];
+  float n;
+  {
+    Coord nb = c;
+    nb.x[MU] = c.x[MU] + 1 == g.L[MU] ? 0 : c.x[MU] + 1;
+    load_spinor_f2<P>(sp, n, in, in_norm, cb_index(g, nb), g.stride);
+    project_f2<MU, SF>(h, sp);
+    scale_f2<P>(h, n);
+    matvec_sm<TX>(uh, lsm, 2 * MU, s, h);
+    reconstruct_f2<MU, SF>(acc, uh);
+  }
+  {
+    Coord nb = c;
+    nb.x[MU] = c.x[MU] == 0 ? g.L[MU] - 1 : c.x[MU] - 1;
+    load_spinor_f2<P>(sp, n, in, in_norm, cb_index(g, nb), g.stride);
+    project_f2<MU, SB>(h, sp);
+    scale_f2<P>(h, n);
+    matvec_sm<TX>(uh, lsm, 2 * MU + 1, s, h);
+    reconstruct_f2<MU, SB>(acc, uh);
+  }
+}
+
 // Grid: one dimension, right-hand-side groups fastest (block b covers sites (b / ng) * TX ... and
 // right-hand sides (b % ng) * NRB ...), so the groups that share a site range run together and
 // their link reads after the first come from L2.  MINB caps the registers (MINB resident blocks).
@@ -297,6 +383,13 @@ __global__ void __launch_bounds__(TX * NRB, MINB) hop_kernel(const HopArgs a) {
   const int idx = sblock * TX + (tid % TX);
   const Geom& g = a.g;
   const bool active = idx < g.Vh && rhs < a.nrhs;
+  // 8 x 9 x 32 x 16 B = 36 KiB of static shared memory for 32-site blocks
+  constexpr bool kShared = NRB > 1 && TX == 32 && std::is_same<T, float>::value;
+  __shared__ float4 lsm[kShared ? 8 : 1][9][kShared ? TX : 1];
+  if constexpr (kShared) {
+    stage_links<P, RECON, TX>(lsm, a, sblock);
+    __syncthreads();
+  }
   double local = 0.0;
   if (active) {
     Coord c = cb_coords(g, idx, a.out_parity);
@@ -307,10 +400,18 @@ __global__ void __launch_bounds__(TX * NRB, MINB) hop_kernel(const HopArgs a) {
       float2 accf[12];
 #pragma unroll
       for (int k = 0; k < 12; ++k) accf[k] = make_float2(0.f, 0.f);
-      hop_dir_f2<P, RECON, 0, DAG>(accf, a, c, idx, in, in_norm);
-      hop_dir_f2<P, RECON, 1, DAG>(accf, a, c, idx, in, in_norm);
-      hop_dir_f2<P, RECON, 2, DAG>(accf, a, c, idx, in, in_norm);
-      hop_dir_f2<P, RECON, 3, DAG>(accf, a, c, idx, in, in_norm);
+      if constexpr (kShared) {
+        const int s = tid % TX;
+        hop_dir_sm<P, 0, DAG, TX>(accf, lsm, s, a, c, in, in_norm);
+        hop_dir_sm<P, 1, DAG, TX>(accf, lsm, s, a, c, in, in_norm);
+        hop_dir_sm<P, 2, DAG, TX>(accf, lsm, s, a, c, in, in_norm);
+        hop_dir_sm<P, 3, DAG, TX>(accf, lsm, s, a, c, in, in_norm);
+      } else {
+        hop_dir_f2<P, RECON, 0, DAG>(accf, a, c, idx, in, in_norm);
+        hop_dir_f2<P, RECON, 1, DAG>(accf, a, c, idx, in, in_norm);
+        hop_dir_f2<P, RECON, 2, DAG>(accf, a, c, idx, in, in_norm);
+        hop_dir_f2<P, RECON, 3, DAG>(accf, a, c, idx, in, in_norm);
+      }
 #pragma unroll
       for (int k = 0; k < 12; ++k) acc[k] = {accf[k].x, accf[k].y};
     } else {

@@ -338,9 +338,12 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
     GBC_CUDA(cudaMemcpyAsync(c->d_kcoef, c->h_kcoef, sizeof(double2) * rows * n, cudaMemcpyHostToDevice, s));
   };
   int total = 0;
+  Spinor tea = sub(workspace(c, 384, pa, n), 0, n);
+  std::vector<double> prev_beta(n, HUGE_VAL);
   while (total < maxit) {
-    // r = b - A x
-    apply_A(x, w);
+    // r = b - A x with the operator in the vectors' precision: each restart is a refinement step,
+    // so the cycles may run on the cheaper sloppy operator
+    apply_meo(c, pa, false, x, w, tea, false);
     blas_xmy_norm2(g, b, w, red(c), s);
     std::vector<double> rr = fetch(c, 1, n);
     std::vector<double> beta(n);
@@ -352,6 +355,9 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
         done[i] = 1;
       }
       if (!done[i] && beta[i] <= tol * std::sqrt(bb[i])) done[i] = 1;
+      // a cycle that no longer reduces the true residual has reached the precision floor
+      if (!done[i] && beta[i] > 0.9 * prev_beta[i]) done[i] = 1;
+      prev_beta[i] = beta[i];
       all &= done[i] != 0;
     }
     if (all) break;

@@ -26,7 +26,9 @@ SYS_MEO, SYS_MDAGM, SYS_FULL = range(3)
 # every entry point include/gbclover.h declares
 EXPORTS = ["gbc_create", "gbc_destroy", "gbc_strerror", "gbc_last_error", "gbc_load_gauge", "gbc_load_clover",
            "gbc_get_clover", "gbc_apply", "gbc_solve", "gbc_solve_device", "gbc_load_precond",
-           "gbc_gauge_synthetic", "gbc_time_operator", "gbc_tune_report"]
+           "gbc_gauge_synthetic", "gbc_time_operator", "gbc_tune_report",
+           "gbc_precond_init", "gbc_precond_save", "gbc_precond_weights", "gbc_precond_set_weights",
+           "gbc_precond_apply", "gbc_precond_loss_grad", "gbc_precond_train"]
 
 
 class Geom(C.Structure):
@@ -90,6 +92,14 @@ def load(path=LIB_PATH):
                                      C.POINTER(Result)]
     lib.gbc_load_precond.argtypes = [C.c_void_p, C.c_char_p]
     lib.gbc_time_operator.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp]
+    fp = C.POINTER(C.c_float)
+    lib.gbc_precond_init.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_ulonglong]
+    lib.gbc_precond_save.argtypes = [C.c_void_p, C.c_char_p]
+    lib.gbc_precond_weights.argtypes = [C.c_void_p, fp, C.c_int, C.POINTER(C.c_int)]
+    lib.gbc_precond_set_weights.argtypes = [C.c_void_p, fp, C.c_int]
+    lib.gbc_precond_apply.argtypes = [C.c_void_p, C.c_int, dp, dp]
+    lib.gbc_precond_loss_grad.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, fp, C.c_int]
+    lib.gbc_precond_train.argtypes = [C.c_void_p, C.c_int, dp, dp, C.c_int, C.c_int, C.c_double, C.c_ulonglong, dp]
     lib.gbc_gauge_synthetic.argtypes = [C.POINTER(C.c_int), C.c_double, C.c_ulonglong, C.c_int, C.c_double,
                                         C.POINTER(C.c_int), C.c_int, dp]
     _lib = lib
@@ -227,3 +237,50 @@ class Context:
 
     def load_precond(self, path):
         self._check(self.lib.gbc_load_precond(self.h, path.encode()), "load_precond")
+
+    # ---- learned preconditioner -------------------------------------------------------------
+    def precond_init(self, hidden=12, layers=4, seed=0):
+        self._check(self.lib.gbc_precond_init(self.h, int(hidden), int(layers), int(seed)), "precond_init")
+
+    def precond_save(self, path):
+        self._check(self.lib.gbc_precond_save(self.h, path.encode()), "precond_save")
+
+    def precond_weights(self):
+        n = C.c_int()
+        self._check(self.lib.gbc_precond_weights(self.h, None, 0, C.byref(n)), "precond_weights")
+        w = np.zeros(n.value, dtype=np.float32)
+        self._check(self.lib.gbc_precond_weights(self.h, w.ctypes.data_as(C.POINTER(C.c_float)), n.value, None),
+                    "precond_weights")
+        return w
+
+    def precond_set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._check(self.lib.gbc_precond_set_weights(self.h, w.ctypes.data_as(C.POINTER(C.c_float)), w.size),
+                    "precond_set_weights")
+
+    def precond_apply(self, x):
+        x = self._fields(x)
+        out = np.zeros_like(x)
+        self._check(self.lib.gbc_precond_apply(self.h, x.shape[0], _dp(out.view(np.float64)),
+                                               _dp(x.view(np.float64))), "precond_apply")
+        return out
+
+    def precond_loss_grad(self, xs, es):
+        xs = self._fields(xs)
+        es = self._fields(es)
+        n = self.precond_weights().size
+        g = np.zeros(n, dtype=np.float32)
+        loss = C.c_double()
+        self._check(self.lib.gbc_precond_loss_grad(self.h, xs.shape[0], _dp(xs.view(np.float64)),
+                                                   _dp(es.view(np.float64)), C.byref(loss),
+                                                   g.ctypes.data_as(C.POINTER(C.c_float)), n), "precond_loss_grad")
+        return loss.value, g
+
+    def precond_train(self, xs, es, epochs=10, batch=8, lr=1e-3, seed=0):
+        xs = self._fields(xs)
+        es = self._fields(es)
+        losses = np.zeros(epochs)
+        self._check(self.lib.gbc_precond_train(self.h, xs.shape[0], _dp(xs.view(np.float64)),
+                                               _dp(es.view(np.float64)), int(epochs), int(batch), float(lr), int(seed),
+                                               _dp(losses)), "precond_train")
+        return losses

@@ -177,8 +177,29 @@ int gbc_time_operator(gbc_ctx* ctx, int op, int prec, int nrhs, int iters, int f
                       double* bytes);
 
 /* ---- learned preconditioner --------------------------------------------------------------- */
-/* Load network weights (versioned binary, see gbc_precond_save) for use inside FGMRES. */
+/* No Chroma counterpart: FGMRESDR_INVERTER takes any factory solver as its preconditioner
+   (syssolver_linop_fgmres_dr.h:173-184); this one is a gauge-covariant linear network K ~ M~^-1
+   of `layers` link-weighted nearest-neighbour layers with `hidden` complex channels per colour
+   (4 or 12), channel mixing on the tensor cores (BF16 in, FP32 accumulate).  Its input/output
+   are odd-site spinors.  Weights file: "GBCW", version 1, layers, hidden, per layer cin, cout,
+   9*cout*cin complex float32, then an FNV-1a 64-bit checksum of everything before it. */
+int gbc_precond_init(gbc_ctx* ctx, int hidden, int layers, unsigned long long seed);
+/* Load network weights for use inside FGMRES (GBC_ERR_PRECOND if missing or corrupt). */
 int gbc_load_precond(gbc_ctx* ctx, const char* path);
+int gbc_precond_save(gbc_ctx* ctx, const char* path);
+/* Weights as interleaved (re, im) floats, layer after layer, W[l][(d*cout + o)*cin + i] with
+   d = 0 self, 1 + 2 mu the +mu hop U_mu(x) h(x+mu), 2 + 2 mu the -mu hop U_mu(x-mu)^dag h(x-mu). */
+int gbc_precond_weights(gbc_ctx* ctx, float* out, int capacity, int* count);
+int gbc_precond_set_weights(gbc_ctx* ctx, const float* in, int count);
+/* out = K(in) for nrhs host spinors (odd sites; even sites of out set to zero). */
+int gbc_precond_apply(gbc_ctx* ctx, int nrhs, double* out, const double* in);
+/* loss = sum_b |K(in_b) - target_b|^2 / |target_b|^2 over odd sites, and dL/dRe W + i dL/dIm W. */
+int gbc_precond_loss_grad(gbc_ctx* ctx, int nb, const double* in, const double* target, double* loss, float* grad,
+                          int capacity);
+/* Adam on minibatches of (input, target) pairs on the current gauge field (forward and backward
+   kernels on the device); loss_per_epoch[epochs] may be NULL. */
+int gbc_precond_train(gbc_ctx* ctx, int nsamples, const double* in, const double* target, int epochs, int batch,
+                      double lr, unsigned long long seed, double* loss_per_epoch);
 
 /* ---- synthetic inputs ---------------------------------------------------------------------- */
 /* Seeded hot-start links U = reunit(exp(i eps H)), H traceless Hermitian with Gaussian entries,
