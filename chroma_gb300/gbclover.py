@@ -26,7 +26,7 @@ SYS_MEO, SYS_MDAGM, SYS_FULL = range(3)
 # every entry point include/gbclover.h declares
 EXPORTS = ["gbc_create", "gbc_destroy", "gbc_strerror", "gbc_last_error", "gbc_load_gauge", "gbc_load_clover",
            "gbc_get_clover", "gbc_apply", "gbc_solve", "gbc_solve_device", "gbc_load_precond",
-           "gbc_gauge_synthetic", "gbc_time_operator", "gbc_tune_report",
+           "gbc_gauge_synthetic", "gbc_time_operator", "gbc_tune_report", "gbc_apply_meo_noalloc",
            "gbc_precond_init", "gbc_precond_save", "gbc_precond_weights", "gbc_precond_set_weights",
            "gbc_precond_apply", "gbc_precond_loss_grad", "gbc_precond_train"]
 

@@ -176,6 +176,27 @@ int gbc_solve_device(gbc_ctx* ctx, const gbc_solve_params* p, int nrhs, double* 
 int gbc_time_operator(gbc_ctx* ctx, int op, int prec, int nrhs, int iters, int flush_l2, double* seconds,
                       double* bytes);
 
+/* ---- no-allocation operator ----------------------------------------------------------------- */
+/* No counterpart in the reference.  The even-odd operator M~ (as gbc_apply with GBC_OP_MEO and
+   GBC_PREC_DOUBLE) for callers that cannot allocate device memory while they run -- e.g. Chroma
+   on QDP-JIT, whose pool allocator reserves most of the GPU at start-up, or code that must not
+   let a cudaMalloc/cudaFree synchronise the device mid-pipeline.  It allocates nothing: every
+   input and output is a caller-owned device pointer in the canonical host layouts above
+   (links_dev: the hopping-term links, BC and any anisotropy factors applied; clov_dev: packed A
+   on the odd sites; invclov_dev: packed A^-1 on the even sites; in_dev/out_dev: full-lattice
+   spinors, odd sites read/written, even sites of out_dev untouched).  Its one temporary, the
+   even-parity intermediate, lives in a static device array of GBC_NOALLOC_MAX_VH sites per
+   checkerboard (12 MiB) that every GPU which loads the library holds until exit.  Lattices with
+   more than GBC_NOALLOC_MAX_VH sites per checkerboard return GBC_ERR_ARGS with a message on
+   stderr.  The first call on a device looks up that array's device address (once per device,
+   with the device current), so make the first call before any stream capture.  Work is issued
+   on `stream` (a cudaStream_t; NULL = the default stream); every call shares the one array, so
+   calls that overlap on the GPU race -- serialise them. */
+#define GBC_NOALLOC_MAX_VH 65536
+int gbc_apply_meo_noalloc(const gbc_geom* geom, const gbc_action* act, const double* links_dev,
+                          const double* clov_dev, const double* invclov_dev, int isign, double* out_dev,
+                          const double* in_dev, void* stream);
+
 /* ---- learned preconditioner --------------------------------------------------------------- */
 /* No Chroma counterpart: FGMRESDR_INVERTER takes any factory solver as its preconditioner
    (syssolver_linop_fgmres_dr.h:173-184); this one is a gauge-covariant linear network K ~ M~^-1
