@@ -64,7 +64,7 @@ def op_only(args):
                 "dslash64": (G.OP_DSLASH, G.PREC_DOUBLE), "meo16": (G.OP_MEO, G.PREC_HALF)}[args.op_only]
     sec, byts = ctx.time_operator(op, prec, nrhs=args.nrhs, iters=args.iters, flush_l2=True)
     print(json.dumps({"op": args.op_only, "dims": dims, "nrhs": args.nrhs, "seconds": sec, "bytes": byts,
-                      "GBps": byts / sec / 1e9}), flush=True)
+                      "GBps": byts / sec / 1e9, "tuned": ctx.tune_report().strip().splitlines()}), flush=True)
     ctx.close()
 
 

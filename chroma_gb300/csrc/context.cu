@@ -170,6 +170,14 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce
   auto it = c->tuned.find(key);
   if (it != c->tuned.end()) return it->second;
   int best = default_shape(h.nrhs);
+  // GBC_SHAPE=<index into kHopShapes> pins one shape (profiling); ignored when out of range
+  if (const char* fs = getenv("GBC_SHAPE")) {
+    const int si = atoi(fs);
+    if (si >= 0 && si < kNumHopShapes && !(kHopShapes[si].nrb > 1 && kHopShapes[si].nrb > h.nrhs)) {
+      c->tuned[key] = si;
+      return si;
+    }
+  }
   if (c->autotune) {
     cudaEvent_t e0, e1;
     GBC_CUDA(cudaEventCreate(&e0));

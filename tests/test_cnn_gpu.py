@@ -112,6 +112,11 @@ def test_fgmres_with_network_converges(setup):
     from oracle import oracle as O
     dims, ctx, net = setup
     V = int(np.prod(dims))
+    # an untrained network starts as (nearly) the identity map
+    ctx.precond_init(hidden=12, layers=4, seed=11)
     chi = S.z2_noise(dims, 3, cb=1).reshape(1, V, 12)
     psi, res, rc = ctx.solve(chi, solver=G.SOLVER_FGMRES, use_precond=1, rsd_target=1e-10)
     assert rc == 0, res
+    op = OracleOp(dims, net.u, 1 / (2 * 0.12) - 4, 1.0)
+    r = chi[0] - op.apply(O.OP_MEO, psi[0])
+    assert np.sqrt(op.norm2(r) / op.norm2(chi[0])) <= 1.05e-10
