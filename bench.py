@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--op-only", default=None, choices=["dslash16", "dslash32", "dslash64", "meo16"],
                     help="profiling mode: set up the workload and time one operator only")
     ap.add_argument("--nrhs", type=int, default=12)
+    ap.add_argument("--recon", type=int, default=12, choices=[12, 18])
     ap.add_argument("--iters", type=int, default=3)
     return ap.parse_args()
 
@@ -58,7 +59,8 @@ def op_only(args):
     from chroma_gb300 import gbclover as G
     dims = tuple(int(x) for x in args.dims.split(",")) if args.dims else DIMS
     links, _ = workload(dims)
-    ctx = G.Context(dims, 1 / (2 * KAPPA) - 4, CSW, t_boundary=-1, max_rhs=max(12, args.nrhs))
+    ctx = G.Context(dims, 1 / (2 * KAPPA) - 4, CSW, t_boundary=-1, max_rhs=max(12, args.nrhs),
+                    sloppy_reconstruct=args.recon)
     ctx.load_gauge(links)
     op, prec = {"dslash16": (G.OP_DSLASH, G.PREC_HALF), "dslash32": (G.OP_DSLASH, G.PREC_SINGLE),
                 "dslash64": (G.OP_DSLASH, G.PREC_DOUBLE), "meo16": (G.OP_MEO, G.PREC_HALF)}[args.op_only]

@@ -341,6 +341,8 @@ int gbc_create(gbc_ctx** out, const gbc_geom* geom, const gbc_action* act, const
     c->max_rhs = c->opts.max_rhs > 0 ? c->opts.max_rhs : 12;
     const char* at = getenv("GBC_AUTOTUNE");
     c->autotune = !(at && at[0] == '0');
+    const char* gr = getenv("GBC_GRAPHS");
+    c->use_graphs = !(gr && gr[0] == '0');
     if (c->max_rhs > 32) throw std::string("max_rhs above 32");
     if (act->aniso) {
       for (int m = 0; m < 4; ++m)

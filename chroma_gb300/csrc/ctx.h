@@ -89,6 +89,7 @@ struct gbc_ctx {
   // autotuned hopping-kernel shapes, keyed by (precision, mode, dagger, reduce, nrhs)
   std::map<long, int> tuned;
   bool autotune = true;
+  bool use_graphs = true;  // CUDA-graph replay of CG iteration blocks (GBC_GRAPHS=0: off)
   std::string tune_log;
 
   // learned preconditioner (opaque, owned by precond.cu)

@@ -123,15 +123,43 @@ CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b
   blas_copy(g, p, r, s);
   bool any = false;
   for (int i = 0; i < n; ++i) any |= hs[i].active != 0;
-  int k = 0;
-  for (k = 1; any && k <= cfg.maxit; ++k) {
+  // One iteration, all scalars on the device: no host round trip inside.
+  auto body = [&]() {
     apply_meo(c, cfg.po, false, p, mp, te, true);     // |mp|^2 -> result
     cg_alpha(c->d_cg, c->d_result, c->d_a, n, s);
     apply_meo(c, cfg.po, true, mp, mmp, te, false);
     blas_cg_update(g, c->d_a, x, p, r, mmp, red(c), s);  // |r|^2 -> result
     cg_beta(c->d_cg, c->d_result, c->d_b, n, s);
-    const bool check = cfg.delta > 0 || (k % cfg.check_every) == 0 || k == cfg.maxit;
-    if (check) {
+    blas_xpay(g, r, c->d_b, p, s);                     // p = r + b p (b = 0 once converged)
+  };
+  // Blocks of kBlock iterations between host checks, replayed from a CUDA graph captured after
+  // the first (uncaptured) iteration has run the autotuner on every kernel shape it needs.
+  // A right-hand side that converges inside a block is frozen by alpha = beta = 0.
+  constexpr int kBlock = 4;
+  cudaGraphExec_t exec = nullptr;
+  long long graph_launches = 0;
+  int k = 0;
+  while (any && k < cfg.maxit) {
+    const int steps = k == 0 ? 1 : std::min(kBlock, cfg.maxit - k);
+    if (k > 0 && steps == kBlock && c->use_graphs) {
+      if (!exec) {
+        cudaGraph_t graph;
+        const long long l0 = launch_count();
+        GBC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int q = 0; q < kBlock; ++q) body();
+        GBC_CUDA(cudaStreamEndCapture(s, &graph));
+        GBC_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+        cudaGraphDestroy(graph);
+        graph_launches = launch_count() - l0;
+        count_launch(-graph_launches);
+      }
+      GBC_CUDA(cudaGraphLaunch(exec, s));
+      count_launch(graph_launches);
+    } else {
+      for (int q = 0; q < steps; ++q) body();
+    }
+    k += steps;
+    {
       GBC_CUDA(cudaMemcpyAsync(c->h_cg, c->d_cg, sizeof(CGScalars) * n, cudaMemcpyDeviceToHost, s));
       sync(c);
       any = false;
@@ -169,14 +197,13 @@ CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b
           bnew[i] = q.b;
         }
         GBC_CUDA(cudaMemcpyAsync(c->d_cg, hs.data(), sizeof(CGScalars) * n, cudaMemcpyHostToDevice, s));
-        GBC_CUDA(cudaMemcpyAsync(c->d_b, bnew.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
         sync(c);
         ++st.reliable;
       }
       if (!any) break;
     }
-    blas_xpay(g, r, c->d_b, p, s);
   }
+  if (exec) cudaGraphExecDestroy(exec);
   GBC_CUDA(cudaMemcpyAsync(c->h_cg, c->d_cg, sizeof(CGScalars) * n, cudaMemcpyDeviceToHost, s));
   sync(c);
   for (int i = 0; i < n; ++i) {

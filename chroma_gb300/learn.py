@@ -20,13 +20,18 @@ from . import sources as S
 
 
 def training_pairs(ctx, dims, nsamples, seed, cg_iters=50, rsd=1e-10, batch=12):
+    """(r, e) pairs: r = b - M~ x_k and e = x* - x_k after cg_iters CGNE iterations from zero
+    (cg_iters = 0 gives the full-inverse pairs (b, M~^-1 b))."""
     V = int(np.prod(dims))
     rs, es = [], []
     for k0 in range(0, nsamples, batch):
         nb = min(batch, nsamples - k0)
         b = np.stack([S.gaussian(dims, seed * 100003 + k0 + k, cb=1).reshape(V, 12) for k in range(nb)])
-        xk, _, _ = ctx.solve(b, solver=G.SOLVER_CG, max_iter=cg_iters, rsd_target=1e-30, raise_on_error=False)
         xs, res, rc = ctx.solve(b, solver=G.SOLVER_MIXED, rsd_target=rsd)
+        if cg_iters > 0:
+            xk, _, _ = ctx.solve(b, solver=G.SOLVER_CG, max_iter=cg_iters, rsd_target=1e-30, raise_on_error=False)
+        else:
+            xk = np.zeros_like(b)
         r = b - ctx.apply(G.OP_MEO, xk, +1, 1, G.PREC_DOUBLE)
         e = xs - xk
         par = S.parity(dims)
@@ -38,7 +43,7 @@ def training_pairs(ctx, dims, nsamples, seed, cg_iters=50, rsd=1e-10, batch=12):
 
 
 def train(dims, kappa, csw, eps=0.3, configs=8, samples=32, cg_iters=50, seed=1000, rounds=4, epochs=5, batch=8,
-          lr=2e-3, hidden=12, layers=4, out=None, log=print):
+          lr=2e-3, hidden=12, layers=4, out=None, log=print, full_pairs=0):
     mass = 1 / (2 * kappa) - 4
     ctx = G.Context(dims, mass, csw, t_boundary=-1, max_rhs=12)
     ctx.precond_init(hidden=hidden, layers=layers, seed=seed)
@@ -48,8 +53,13 @@ def train(dims, kappa, csw, eps=0.3, configs=8, samples=32, cg_iters=50, seed=10
         links = G.gauge_synthetic(dims, eps, seed + cfg, t_boundary=-1)
         ctx.load_gauge(links)
         r, e = training_pairs(ctx, dims, samples, seed + cfg, cg_iters)
+        if full_pairs:
+            # as many full-inverse pairs: the network must also act sensibly on every mode that
+            # FGMRES feeds it, not only on the low modes
+            rf, ef = training_pairs(ctx, dims, full_pairs, seed + cfg + 7919, 0)
+            r, e = np.concatenate([r, rf]), np.concatenate([e, ef])
         data.append((links, r, e))
-        log(f"config {cfg}: {samples} pairs, |e|/|r| = {np.linalg.norm(e) / np.linalg.norm(r):.3f}")
+        log(f"config {cfg}: {len(r)} pairs, |e|/|r| = {np.linalg.norm(e) / np.linalg.norm(r):.3f}")
     history = []
     for rnd in range(rounds):
         for cfg, (links, r, e) in enumerate(data):
@@ -85,11 +95,13 @@ def main():
     ap.add_argument("--rounds", type=int, default=4)
     ap.add_argument("--epochs", type=int, default=5)
     ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--cg-iters", type=int, default=50)
+    ap.add_argument("--full-pairs", type=int, default=0)
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
     dims = tuple(int(x) for x in a.dims.split(","))
     ctx, hist = train(dims, a.kappa, a.csw, configs=a.configs, samples=a.samples, rounds=a.rounds, epochs=a.epochs,
-                      lr=a.lr, out=a.out)
+                      lr=a.lr, out=a.out, cg_iters=a.cg_iters, full_pairs=a.full_pairs)
     links = G.gauge_synthetic(dims, 0.3, 999_999, t_boundary=-1)
     ctx.load_gauge(links)
     print(json.dumps({"loss_history": hist, "ablation": ablation(ctx, dims)}))
