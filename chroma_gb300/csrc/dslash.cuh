@@ -371,14 +371,29 @@ __device__ __forceinline__ void hop_dir_sm(float2 (&acc)[12], const float4 (*lsm
 // Grid: one dimension, right-hand-side groups fastest (block b covers sites (b / ng) * TX ... and
 // right-hand sides (b % ng) * NRB ...), so the groups that share a site range run together and
 // their link reads after the first come from L2.  MINB caps the registers (MINB resident blocks).
+template <typename P, int RECON, int MODE, bool DAG, bool REDUCE, int TX, int NRB>
+__device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group);
+
 template <typename P, int RECON, int MODE, bool DAG, bool REDUCE, int TX, int NRB, int MINB>
 __global__ void __launch_bounds__(TX * NRB, MINB) hop_kernel(const HopArgs a) {
+  const int ng = (a.nrhs + NRB - 1) / NRB;
+  const int sblock = blockIdx.x / ng;
+  hop_body<P, RECON, MODE, DAG, REDUCE, TX, NRB>(a, sblock, blockIdx.x - sblock * ng);
+}
+
+// One launch over several independent lattices (each its own HopArgs: geometry, fields,
+// partials): block b works on lattice work[b].x, site block work[b].y.
+template <typename P, int RECON, int MODE, bool DAG, bool REDUCE>
+__global__ void __launch_bounds__(128) hop_kernel_multi(const HopArgs* __restrict__ args, const int2* __restrict__ work) {
+  const int2 w = work[blockIdx.x];
+  hop_body<P, RECON, MODE, DAG, REDUCE, 128, 1>(args[w.x], w.y, 0);
+}
+
+template <typename P, int RECON, int MODE, bool DAG, bool REDUCE, int TX, int NRB>
+__device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group) {
   using T = typename P::real;
   const int tid = threadIdx.x;
   const int rl = tid / TX;
-  const int ng = (a.nrhs + NRB - 1) / NRB;
-  const int sblock = blockIdx.x / ng;
-  const int group = blockIdx.x - sblock * ng;
   const int rhs = group * NRB + rl;
   const int idx = sblock * TX + (tid % TX);
   const Geom& g = a.g;

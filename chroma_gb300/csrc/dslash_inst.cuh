@@ -48,4 +48,28 @@ static int hop_recon(int recon, int mode, bool reduce, const HopArgs& a, HopShap
   return -1;
 }
 
+// several lattices in one launch (work table of (lattice, site block), 128-site blocks)
+template <typename P, int RECON, bool DAG>
+static int hop_multi_mode(int mode, bool reduce, const HopArgs* args, const int2* work, int nwork, cudaStream_t s) {
+  switch (mode) {
+    case HOP_PLAIN: hop_kernel_multi<P, RECON, HOP_PLAIN, DAG, false><<<nwork, 128, 0, s>>>(args, work); return nwork;
+    case HOP_CLOV: hop_kernel_multi<P, RECON, HOP_CLOV, DAG, false><<<nwork, 128, 0, s>>>(args, work); return nwork;
+    case HOP_XPAY:
+      if (reduce) hop_kernel_multi<P, RECON, HOP_XPAY, DAG, true><<<nwork, 128, 0, s>>>(args, work);
+      else hop_kernel_multi<P, RECON, HOP_XPAY, DAG, false><<<nwork, 128, 0, s>>>(args, work);
+      return nwork;
+  }
+  return -1;
+}
+
+template <typename P, bool DAG>
+static int hop_multi_recon(int recon, int mode, bool reduce, const HopArgs* args, const int2* work, int nwork,
+                           cudaStream_t s) {
+  if (recon == 18) return hop_multi_mode<P, 18, DAG>(mode, reduce, args, work, nwork, s);
+#if GBC_RECON12
+  if (recon == 12) return hop_multi_mode<P, 12, DAG>(mode, reduce, args, work, nwork, s);
+#endif
+  return -1;
+}
+
 }  // namespace gbc

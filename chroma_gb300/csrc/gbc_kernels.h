@@ -72,6 +72,23 @@ int hop_launch_d(int recon, int mode, bool dag, bool reduce, const HopArgs& a, H
 int hop_launch_s(int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
 int hop_launch_h(int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
 
+// One launch over several lattices: args[l] in device memory, work[b] = (lattice, 128-site block).
+int hop_multi_launch_d(int recon, int mode, bool dag, bool reduce, const HopArgs* args, const int2* work, int nwork,
+                       cudaStream_t s);
+int hop_multi_launch_s(int recon, int mode, bool dag, bool reduce, const HopArgs* args, const int2* work, int nwork,
+                       cudaStream_t s);
+int hop_multi_launch_h(int recon, int mode, bool dag, bool reduce, const HopArgs* args, const int2* work, int nwork,
+                       cudaStream_t s);
+inline int hop_multi_launch(int prec, int recon, int mode, bool dag, bool reduce, const HopArgs* args,
+                            const int2* work, int nwork, cudaStream_t s) {
+  switch (prec) {
+    case PREC_DOUBLE: return hop_multi_launch_d(recon, mode, dag, reduce, args, work, nwork, s);
+    case PREC_SINGLE: return hop_multi_launch_s(recon, mode, dag, reduce, args, work, nwork, s);
+    case PREC_HALF: return hop_multi_launch_h(recon, mode, dag, reduce, args, work, nwork, s);
+  }
+  return -1;
+}
+
 inline int hop_launch(int prec, int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh,
                       cudaStream_t s) {
   switch (prec) {

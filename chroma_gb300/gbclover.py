@@ -28,7 +28,8 @@ EXPORTS = ["gbc_create", "gbc_destroy", "gbc_strerror", "gbc_last_error", "gbc_l
            "gbc_get_clover", "gbc_apply", "gbc_solve", "gbc_solve_device", "gbc_load_precond",
            "gbc_gauge_synthetic", "gbc_time_operator", "gbc_tune_report", "gbc_apply_meo_noalloc",
            "gbc_precond_init", "gbc_precond_save", "gbc_precond_weights", "gbc_precond_set_weights",
-           "gbc_precond_apply", "gbc_precond_loss_grad", "gbc_precond_train"]
+           "gbc_precond_apply", "gbc_precond_loss_grad", "gbc_precond_train", "gbc_batch_create",
+           "gbc_batch_destroy", "gbc_batch_solve", "gbc_batch_last_error"]
 
 
 class Geom(C.Structure):
@@ -102,6 +103,13 @@ def load(path=LIB_PATH):
     lib.gbc_precond_train.argtypes = [C.c_void_p, C.c_int, dp, dp, C.c_int, C.c_int, C.c_double, C.c_ulonglong, dp]
     lib.gbc_gauge_synthetic.argtypes = [C.POINTER(C.c_int), C.c_double, C.c_ulonglong, C.c_int, C.c_double,
                                         C.POINTER(C.c_int), C.c_int, dp]
+    lib.gbc_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]
+    lib.gbc_batch_destroy.argtypes = [C.c_void_p]
+    lib.gbc_batch_destroy.restype = None
+    lib.gbc_batch_solve.argtypes = [C.c_void_p, C.POINTER(SolveParams), C.POINTER(dp), C.POINTER(dp),
+                                    C.POINTER(Result)]
+    lib.gbc_batch_last_error.restype = C.c_char_p
+    lib.gbc_batch_last_error.argtypes = [C.c_void_p]
     _lib = lib
     return lib
 
@@ -284,3 +292,42 @@ class Context:
                                                _dp(es.view(np.float64)), int(epochs), int(batch), float(lr), int(seed),
                                                _dp(losses)), "precond_train")
         return losses
+
+
+class Batch:
+    """Independent lattices solved together (gbc_batch_*): one stencil launch covers all of them."""
+
+    def __init__(self, contexts):
+        self.lib = load()
+        self.contexts = list(contexts)
+        arr = (C.c_void_p * len(self.contexts))(*[c.h.value for c in self.contexts])
+        h = C.c_void_p()
+        rc = self.lib.gbc_batch_create(C.byref(h), len(self.contexts), arr)
+        if rc != GBC_OK:
+            raise GBCError(rc, "gbc_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, chis, rsd_target=1e-10, max_iter=10000, delta=0.1, sloppy_precision=0, inner_tol=0.0):
+        n = len(self.contexts)
+        chis = [np.ascontiguousarray(x, dtype=np.complex128).reshape(ctx.V, 12) for x, ctx in zip(chis, self.contexts)]
+        psis = [np.zeros_like(x) for x in chis]
+        p = SolveParams(SOLVER_MIXED, SYS_MEO, float(rsd_target), int(max_iter), float(delta), 10.0,
+                        int(sloppy_precision), float(inner_tol), 0, 16, 0, 1)
+        cp = (C.POINTER(C.c_double) * n)(*[_dp(x.view(np.float64)) for x in chis])
+        pp = (C.POINTER(C.c_double) * n)(*[_dp(x.view(np.float64)) for x in psis])
+        res = (Result * n)()
+        rc = self.lib.gbc_batch_solve(self.h, C.byref(p), pp, cp, res)
+        if rc != GBC_OK:
+            raise GBCError(rc, "batch_solve: " + self.lib.gbc_batch_last_error(self.h).decode())
+        return psis, [r.as_dict() for r in res]

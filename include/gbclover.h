@@ -165,6 +165,19 @@ int gbc_solve(gbc_ctx* ctx, const gbc_solve_params* p, int nrhs, double* psi, co
 int gbc_solve_device(gbc_ctx* ctx, const gbc_solve_params* p, int nrhs, double* psi_dev, const double* chi_dev,
                      gbc_result* res);
 
+/* ---- batches of independent lattices ------------------------------------------------------- */
+/* No Chroma counterpart (Chroma solves one lattice at a time).  A batch groups contexts of
+   different lattices (each loaded with its gauge field, same sloppy reconstruction); a batch solve
+   runs the outer FP64 defect correction per lattice and the inner reliable-update CGNE for all
+   lattices together, each stencil application one launch over a work table of (lattice, block)
+   pairs.  psi[l], chi[l]: host spinors of lattice l (odd sites, as GBC_SYS_MEO). */
+typedef struct gbc_batch gbc_batch;
+int gbc_batch_create(gbc_batch** batch, int n, gbc_ctx* const* ctxs);
+void gbc_batch_destroy(gbc_batch* batch);
+int gbc_batch_solve(gbc_batch* batch, const gbc_solve_params* p, double* const* psi, const double* const* chi,
+                    gbc_result* res);
+const char* gbc_batch_last_error(gbc_batch* batch);
+
 /* ---- measurement (the timing loops of Chroma's t_clover.cc:16-212 / t_lwldslash_sse.cc:20-215) */
 /* Times `iters` applications of op (GBC_OP_DSLASH: one hopping launch; GBC_OP_MEO: the two fused
    launches of M~) on device-resident pseudo-random fields of nrhs right-hand sides in precision
