@@ -147,7 +147,7 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
     }
     struct L {
       Spinor x, bd, rd, t1, t2, ted, rs, es, rhs, r, pv, mp, mmp, te, th1, teh;
-      double bb = 0, rr = 0;
+      double bb = 0, rr = 0, prev_rr = HUGE_VAL;
       int done = 0, iters = 0, outer = 0, status = GBC_OK;
     };
     std::vector<L> lat(n);
@@ -235,11 +235,27 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
       for (int l = 0; l < n; ++l) {
         L& q = lat[l];
         if (q.done) continue;
+        if (std::isfinite(q.prev_rr) && !(q.rr <= q.prev_rr)) {
+          // the last correction left the FP64 residual larger (an inner solve that broke down):
+          // take it back and stop this lattice with the better iterate
+          gbc_ctx* c = b->ctx[l];
+          c->h_coef[0] = make_double2(-1.0, 0.0);
+          c->h_coef[1] = make_double2(1.0, 0.0);
+          GBC_CUDA(cudaMemcpyAsync(c->d_ca, c->h_coef, sizeof(double2), cudaMemcpyHostToDevice, s));
+          GBC_CUDA(cudaMemcpyAsync(c->d_cb, c->h_coef + 1, sizeof(double2), cudaMemcpyHostToDevice, s));
+          blas_axpby(c->g, c->d_ca, q.es, c->d_cb, q.x, s);
+          GBC_CUDA(cudaStreamSynchronize(s));
+          q.rr = q.prev_rr;
+          q.status = GBC_ERR_NOT_CONVERGED;
+          q.done = 1;
+          continue;
+        }
         if (!std::isfinite(q.rr)) {
           q.status = GBC_ERR_NONFINITE;
           q.done = 1;
           continue;
         }
+        q.prev_rr = q.rr;
         if (q.rr <= p.rsd_target * p.rsd_target * q.bb) q.done = 1;
         else {
           all = false;
@@ -263,14 +279,15 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
         GBC_CUDA(cudaMemcpyAsync(&rr0[l], c->d_result, sizeof(double), cudaMemcpyDeviceToHost, s));
       }
       GBC_CUDA(cudaStreamSynchronize(s));
-      std::vector<double> maxrr(n);
+      std::vector<double> maxrr(n), at_update(n), last_nr(n, HUGE_VAL);
+      std::vector<int> stall(n, 0);
       for (int l = 0; l < n; ++l) {
         L& q = lat[l];
         CGScalars st{};
         st.c = st.cp = st.c_prev = rr0[l];
         st.rsd_sq = itol * itol * rr0[l];
         st.active = !q.done && rr0[l] > 0;
-        maxrr[l] = std::sqrt(rr0[l]);
+        maxrr[l] = at_update[l] = std::sqrt(rr0[l]);
         GBC_CUDA(cudaMemcpyAsync(b->ctx[l]->d_cg, &st, sizeof(CGScalars), cudaMemcpyHostToDevice, s));
       }
       GBC_CUDA(cudaStreamSynchronize(s));
@@ -312,6 +329,7 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
           const double rn = std::sqrt(hs[l].cp);
           maxrr[l] = std::max(maxrr[l], rn);
           if (rn < p.delta * maxrr[l]) trigger = true;
+          if (rn > at_update[l]) trigger = true;  // the recurrence drifted up: check the true residual
         }
         if (any && trigger) {
           // reliable update for every active lattice: r = rhs - M~^dag M~ e (accumulator precision)
@@ -329,8 +347,15 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
           for (int l = 0; l < n; ++l) {
             if (!hs[l].active) continue;
             hs[l].c = hs[l].cp = nr[l];
-            maxrr[l] = std::sqrt(nr[l]);
-            if (!(nr[l] > hs[l].rsd_sq)) hs[l].active = 0;
+            maxrr[l] = at_update[l] = std::sqrt(nr[l]);
+            // three reliable updates in a row that fail to halve the true residual: the accumulator
+            // precision's floor is reached, the FP64 outer loop takes over
+            stall[l] = nr[l] > 0.25 * last_nr[l] ? stall[l] + 1 : 0;
+            last_nr[l] = nr[l];
+            if (!(nr[l] > hs[l].rsd_sq) || stall[l] >= 3) {
+              hs[l].active = 0;
+              hs[l].b = 0;
+            }
             GBC_CUDA(cudaMemcpyAsync(b->ctx[l]->d_cg, &hs[l], sizeof(CGScalars), cudaMemcpyHostToDevice, s));
           }
           GBC_CUDA(cudaStreamSynchronize(s));

@@ -107,7 +107,7 @@ CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b
   std::vector<double> rr = fetch(c, 1, n);
   std::vector<double> bb = norm2(c, b);
   std::vector<CGScalars> hs(n);
-  std::vector<double> maxrr(n), last_rel(n, HUGE_VAL);
+  std::vector<double> maxrr(n), last_rel(n, HUGE_VAL), at_update(n);
   std::vector<int> stall(n, 0);
   for (int i = 0; i < n; ++i) {
     CGScalars& q = hs[i];
@@ -117,7 +117,7 @@ CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b
     q.rsd_sq = cfg.rsd * cfg.rsd * bb[i];
     q.active = active[i] && std::isfinite(rr[i]) && rr[i] > q.rsd_sq;
     if (!std::isfinite(rr[i]) || !std::isfinite(bb[i])) st.status[i] = GBC_ERR_NONFINITE;
-    maxrr[i] = std::sqrt(rr[i]);
+    maxrr[i] = at_update[i] = std::sqrt(rr[i]);
   }
   GBC_CUDA(cudaMemcpyAsync(c->d_cg, hs.data(), sizeof(CGScalars) * n, cudaMemcpyHostToDevice, s));
   blas_copy(g, p, r, s);
@@ -171,6 +171,11 @@ CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b
         double rn = std::sqrt(c->h_cg[i].cp);
         maxrr[i] = std::max(maxrr[i], rn);
         if (cfg.delta > 0 && rn < cfg.delta * maxrr[i]) trigger = true;
+        // an iterated residual back above its value at the last reliable update means the
+        // recurrence has lost touch with the true residual (the accumulator precision's floor):
+        // check it now, so that the stall test below can end this right-hand side instead of
+        // letting the recurrence drift
+        if (rn > at_update[i]) trigger = true;
       }
       if (any && trigger) {
         // reliable update: r = b - A^dag A x from the accumulator-precision operator
@@ -183,7 +188,7 @@ CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b
           if (q.active) {
             q.b = q.c_prev > 0 ? nr[i] / q.c_prev : 0.0;
             q.c = q.cp = nr[i];
-            maxrr[i] = std::sqrt(nr[i]);
+            maxrr[i] = at_update[i] = std::sqrt(nr[i]);
             // the true residual has hit the accumulator precision's floor when three reliable
             // updates in a row fail to halve it: stop this right-hand side (the outer FP64 loop
             // takes over from there)
@@ -636,6 +641,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
       }
     const int max_outer = 50;
     int total = 0;
+    std::vector<double> prev_rr(n, HUGE_VAL);
     for (int it = 0; it <= max_outer; ++it) {
       // FP64 residual
       if (it == 0 && p.zero_guess) {
@@ -646,6 +652,27 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
         blas_xmy_norm2(g, chi, rd, red(c), s);
       }
       std::vector<double> rr = fetch(c, 1, n);
+      // A correction that left the FP64 residual larger than before (an inner solve that broke
+      // down) is taken back, and that right-hand side stops with the better iterate.
+      bool revert = false;
+      for (int i = 0; i < n; ++i) {
+        const bool back = !done[i] && std::isfinite(prev_rr[i]) && !(rr[i] <= prev_rr[i]);
+        c->h_coef[i] = make_double2(back ? -1.0 : 0.0, 0.0);
+        c->h_coef[n + i] = make_double2(1.0, 0.0);
+        if (back) {
+          revert = true;
+          done[i] = 1;
+          rr[i] = prev_rr[i];
+          if (status[i] == GBC_OK) status[i] = GBC_ERR_NOT_CONVERGED;
+        }
+      }
+      if (revert) {
+        GBC_CUDA(cudaMemcpyAsync(c->d_ca, c->h_coef, sizeof(double2) * n, cudaMemcpyHostToDevice, s));
+        GBC_CUDA(cudaMemcpyAsync(c->d_cb, c->h_coef + n, sizeof(double2) * n, cudaMemcpyHostToDevice, s));
+        blas_axpby(g, c->d_ca, es, c->d_cb, psi, s);  // psi = psi - es for those right-hand sides
+        sync(c);
+      }
+      for (int i = 0; i < n; ++i) prev_rr[i] = rr[i];
       bool all = true;
       double worst = 0.0;
       for (int i = 0; i < n; ++i) {

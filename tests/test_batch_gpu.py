@@ -32,10 +32,43 @@ def test_batch_of_uneven_lattices():
             rel = np.sqrt(ops[k].norm2(r) / ops[k].norm2(chis[k]))
             assert rel <= 1.05e-10, (lattices[k], rel, res[k])
             assert res[k]["status"] == 0
-            # the same answer as the single-lattice solver
-            single, _, _ = ctxs[k].solve(chis[k].reshape(1, -1, 12), solver=G.SOLVER_MIXED, rsd_target=1e-12)
+            # the same answer as the single-lattice FP64 CG
+            single, _, _ = ctxs[k].solve(chis[k].reshape(1, -1, 12), solver=G.SOLVER_CG, rsd_target=1e-12)
             assert np.linalg.norm(psis[k] - single[0]) / np.linalg.norm(single[0]) < 1e-8
     finally:
         batch.close()
         for c in ctxs:
             c.close()
+
+
+@pytest.mark.parametrize("sloppy", [G.PREC_HALF, G.PREC_SINGLE], ids=["f16", "f32"])
+def test_tight_target_below_inner_precision(sloppy):
+    """A target of 1e-12 asks the inner CGNE for reductions below what its FP32 accumulators can
+    hold on this lattice; the inner solve must stop at that floor (not drift) and the FP64 outer
+    loop must still reach the target, for the single-lattice and the batched solver."""
+    from oracle import Oracle, OracleOp
+    from oracle import oracle as O
+    o = Oracle()
+    kappa, csw = 0.124, 1.5
+    mass = 1 / (2 * kappa) - 4
+    dims = (4, 6, 8, 10)
+    u = o.apply_bc(dims, o.gauge_hot(dims, 0.3, 503), (1, 1, 1, -1))
+    op = OracleOp(dims, u, mass, csw)
+    chi = S.z2_noise(dims, 603, cb=1).reshape(-1, 12)
+    ctx = G.Context(dims, mass, csw, t_boundary=-1, max_rhs=1, sloppy_precision=sloppy)
+    ctx.load_gauge(u)
+    try:
+        psi, res, rc = ctx.solve(chi.reshape(1, -1, 12), solver=G.SOLVER_MIXED, rsd_target=1e-12)
+        r = chi - op.apply(O.OP_MEO, psi[0])
+        assert np.sqrt(op.norm2(r) / op.norm2(chi)) <= 1.05e-12, res
+        assert rc == 0 and res[0]["status"] == 0
+        batch = G.Batch([ctx])
+        try:
+            psis, bres = batch.solve([chi], rsd_target=1e-12, sloppy_precision=sloppy)
+        finally:
+            batch.close()
+        r = chi - op.apply(O.OP_MEO, psis[0])
+        assert np.sqrt(op.norm2(r) / op.norm2(chi)) <= 1.05e-12, bres
+        assert bres[0]["status"] == 0
+    finally:
+        ctx.close()
