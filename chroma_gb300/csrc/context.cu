@@ -173,7 +173,7 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce
   // GBC_SHAPE=<index into kHopShapes> pins one shape (profiling); ignored when out of range
   if (const char* fs = getenv("GBC_SHAPE")) {
     const int si = atoi(fs);
-    if (si >= 0 && si < kNumHopShapes && !(kHopShapes[si].nrb > 1 && kHopShapes[si].nrb > h.nrhs)) {
+    if (si >= 0 && si < kNumHopShapes && hop_shape_valid(kHopShapes[si], prec, h.nrhs, h.g.L[3])) {
       c->tuned[key] = si;
       return si;
     }
@@ -185,7 +185,7 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce
     float best_ms = 1e30f;
     for (int si = 0; si < kNumHopShapes; ++si) {
       const HopShape sh = kHopShapes[si];
-      if (sh.nrb > 1 && sh.nrb > h.nrhs) continue;  // a block would be mostly idle
+      if (!hop_shape_valid(sh, prec, h.nrhs, h.g.L[3])) continue;
       if (hop_launch(prec, recon, mode, dag, reduce, h, sh, c->stream) < 0) continue;
       if (cudaPeekAtLastError() != cudaSuccess) {
         cudaGetLastError();  // e.g. too many resources for this shape: not a candidate
@@ -206,9 +206,9 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     char line[160];
-    snprintf(line, sizeof line, "prec=%d mode=%d dag=%d reduce=%d nrhs=%d -> tx=%d nrb=%d minb=%d (%.1f us)\n", prec,
-             mode, dag ? 1 : 0, reduce ? 1 : 0, h.nrhs, kHopShapes[best].tx, kHopShapes[best].nrb,
-             kHopShapes[best].minb, best_ms / 3 * 1e3);
+    snprintf(line, sizeof line, "prec=%d mode=%d dag=%d reduce=%d nrhs=%d -> tx=%d nrb=%d minb=%d pair=%d (%.1f us)\n",
+             prec, mode, dag ? 1 : 0, reduce ? 1 : 0, h.nrhs, kHopShapes[best].tx, kHopShapes[best].nrb,
+             kHopShapes[best].minb, kHopShapes[best].pair, best_ms / 3 * 1e3);
     c->tune_log += line;
   }
   c->tuned[key] = best;

@@ -374,6 +374,71 @@ __device__ __forceinline__ void hop_dir_sm(float2 (&acc)[12], const float4 (*lsm
 template <typename P, int RECON, int MODE, bool DAG, bool REDUCE, int TX, int NRB>
 __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group);
 
+// The MODE epilogue of one output site: out = a D' psi, T (a D' psi) or T self + a D' psi
+// (+ twist), stored in the output precision; returns |out|^2 of the site when REDUCE.
+template <typename P, int MODE, bool DAG, bool REDUCE>
+__device__ __forceinline__ typename P::real hop_epilogue(const HopArgs& a, int rhs, int idx,
+                                                         const cplx<typename P::real> (&acc)[12]) {
+  using T = typename P::real;
+  const Geom& g = a.g;
+  const T coef = (T)a.a;
+  cplx<T> out[12];
+  if constexpr (MODE == HOP_PLAIN) {
+#pragma unroll
+    for (int k = 0; k < 12; ++k) out[k] = coef * acc[k];
+  } else if constexpr (MODE == HOP_CLOV) {
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      T d[6];
+      cplx<T> o[15], x[6], y[6];
+      load_clover_block<P>(d, o, a.clov, idx, g.stride, b);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) x[k] = coef * acc[6 * b + k];
+      clover_block_mul(y, d, o, x);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) out[6 * b + k] = y[k];
+    }
+  } else {  // HOP_XPAY
+    cplx<T> self[12];
+    const char* sp = (const char*)a.self + (size_t)rhs * a.self_rhs_bytes;
+    load_spinor<P>(self, sp, a.self_norm ? a.self_norm + (size_t)rhs * a.norm_rhs_stride : nullptr, idx, g.stride);
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      T d[6];
+      cplx<T> o[15], x[6], y[6];
+      load_clover_block<P>(d, o, a.clov, idx, g.stride, b);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) x[k] = self[6 * b + k];
+      clover_block_mul(y, d, o, x);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        cplx<T> v = y[k];
+        v.re = fmadd(coef, acc[6 * b + k].re, v.re);
+        v.im = fmadd(coef, acc[6 * b + k].im, v.im);
+        out[6 * b + k] = v;
+      }
+    }
+    if (a.twist != 0.0) {
+      // + isign * i * mu * gamma_5 self,  gamma_5 = diag(1, 1, -1, -1)
+      const T tw = (T)(DAG ? -a.twist : a.twist);
+#pragma unroll
+      for (int k = 0; k < 12; ++k) {
+        T s5 = k < 6 ? tw : -tw;
+        out[k] = out[k] + s5 * timesI(self[k]);
+      }
+    }
+  }
+  char* op = (char*)a.out + (size_t)rhs * a.out_rhs_bytes;
+  store_spinor<P>(op, a.out_norm ? a.out_norm + (size_t)rhs * a.norm_rhs_stride : nullptr, idx, g.stride, out);
+  T site = 0;
+  if constexpr (REDUCE) {
+    // site sum in the compute precision (FP64 is slow on this part), block sums in FP64
+#pragma unroll
+    for (int k = 0; k < 12; ++k) site = fmadd(out[k].re, out[k].re, fmadd(out[k].im, out[k].im, site));
+  }
+  return site;
+}
+
 template <typename P, int RECON, int MODE, bool DAG, bool REDUCE, int TX, int NRB, int MINB>
 __global__ void __launch_bounds__(TX * NRB, MINB) hop_kernel(const HopArgs a) {
   const int ng = (a.nrhs + NRB - 1) / NRB;
@@ -437,62 +502,7 @@ __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group
       hop_dir<P, RECON, 2, DAG>(acc, a, c, idx, in, in_norm);
       hop_dir<P, RECON, 3, DAG>(acc, a, c, idx, in, in_norm);
     }
-    const T coef = (T)a.a;
-    cplx<T> out[12];
-    if constexpr (MODE == HOP_PLAIN) {
-#pragma unroll
-      for (int k = 0; k < 12; ++k) out[k] = coef * acc[k];
-    } else if constexpr (MODE == HOP_CLOV) {
-#pragma unroll
-      for (int b = 0; b < 2; ++b) {
-        T d[6];
-        cplx<T> o[15], x[6], y[6];
-        load_clover_block<P>(d, o, a.clov, idx, g.stride, b);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) x[k] = coef * acc[6 * b + k];
-        clover_block_mul(y, d, o, x);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) out[6 * b + k] = y[k];
-      }
-    } else {  // HOP_XPAY
-      cplx<T> self[12];
-      const char* sp = (const char*)a.self + (size_t)rhs * a.self_rhs_bytes;
-      load_spinor<P>(self, sp, a.self_norm ? a.self_norm + (size_t)rhs * a.norm_rhs_stride : nullptr, idx, g.stride);
-#pragma unroll
-      for (int b = 0; b < 2; ++b) {
-        T d[6];
-        cplx<T> o[15], x[6], y[6];
-        load_clover_block<P>(d, o, a.clov, idx, g.stride, b);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) x[k] = self[6 * b + k];
-        clover_block_mul(y, d, o, x);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          cplx<T> v = y[k];
-          v.re = fmadd(coef, acc[6 * b + k].re, v.re);
-          v.im = fmadd(coef, acc[6 * b + k].im, v.im);
-          out[6 * b + k] = v;
-        }
-      }
-      if (a.twist != 0.0) {
-        // + isign * i * mu * gamma_5 self,  gamma_5 = diag(1, 1, -1, -1)
-        const T tw = (T)(DAG ? -a.twist : a.twist);
-#pragma unroll
-        for (int k = 0; k < 12; ++k) {
-          T s5 = k < 6 ? tw : -tw;
-          out[k] = out[k] + s5 * timesI(self[k]);
-        }
-      }
-    }
-    char* op = (char*)a.out + (size_t)rhs * a.out_rhs_bytes;
-    store_spinor<P>(op, a.out_norm ? a.out_norm + (size_t)rhs * a.norm_rhs_stride : nullptr, idx, g.stride, out);
-    if constexpr (REDUCE) {
-      // site sum in the compute precision (FP64 is slow on this part), block sums in FP64
-      T site = 0;
-#pragma unroll
-      for (int k = 0; k < 12; ++k) site = fmadd(out[k].re, out[k].re, fmadd(out[k].im, out[k].im, site));
-      local = (double)site;
-    }
+    local = (double)hop_epilogue<P, MODE, DAG, REDUCE>(a, rhs, idx, acc);
   }
   if constexpr (REDUCE) {
     // warps never straddle two right-hand sides (TX is a multiple of 32)
@@ -507,6 +517,254 @@ __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group
 #pragma unroll
       for (int w = 0; w < TX / 32; ++w) s += wsum[tid * (TX / 32) + w];
       if (r < a.nrhs) a.partials[(size_t)r * a.part_stride + sblock] = s;
+    }
+  }
+}
+
+// ---- fp16 storage, two sites per thread ---------------------------------------------------------
+// The sites A = (x, y, z, t) and B = (x', y, z, t + Lt/2) of the output checkerboard (cb indices
+// i and i + Vh/2, same x/2) share one thread, and every float2 holds one real component of both
+// (.x = A, .y = B).  Complex arithmetic then becomes real FFMA2/FADD2 arithmetic on pairs with no
+// lane swaps or sign shuffles, the factors +-i of the projectors only relabel real and imaginary
+// parts, the fp16 conversions land directly in the pair registers, and the site norm folds into
+// the accumulation FMAs.  Needs Lt even (the checkerboard already needs Lx even).
+struct C2 {
+  float2 r, i;
+};
+
+// a - b on both lanes (sub.rn.f32x2, sm_100 and later)
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+  unsigned long long ra = *reinterpret_cast<unsigned long long*>(&a), rb = *reinterpret_cast<unsigned long long*>(&b),
+                     rd;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+  return *reinterpret_cast<float2*>(&rd);
+}
+
+__device__ __forceinline__ C2 c2_from_h2(uint32_t wa, uint32_t wb) {
+  const __half2 ha = *reinterpret_cast<const __half2*>(&wa);
+  const __half2 hb = *reinterpret_cast<const __half2*>(&wb);
+  return C2{make_float2(__low2float(ha), __low2float(hb)), make_float2(__high2float(ha), __high2float(hb))};
+}
+
+__device__ __forceinline__ C2 c2add(C2 a, C2 b) { return {__fadd2_rn(a.r, b.r), __fadd2_rn(a.i, b.i)}; }
+__device__ __forceinline__ C2 c2sub(C2 a, C2 b) { return {fsub2(a.r, b.r), fsub2(a.i, b.i)}; }
+__device__ __forceinline__ C2 c2addi(C2 a, C2 b) { return {fsub2(a.r, b.i), __fadd2_rn(a.i, b.r)}; }  // a + i b
+__device__ __forceinline__ C2 c2subi(C2 a, C2 b) { return {__fadd2_rn(a.r, b.i), fsub2(a.i, b.r)}; }  // a - i b
+
+// the 12 components of the fp16 spinor at cb sites ja, jb (still divided by their site norms)
+__device__ __forceinline__ void load_spinor_pair(C2 (&s)[12], const void* base, int ja, int jb, int stride) {
+  const uint4* p = reinterpret_cast<const uint4*>(base);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const uint4 va = ldg(p + (size_t)k * stride + ja);
+    const uint4 vb = ldg(p + (size_t)k * stride + jb);
+    s[4 * k + 0] = c2_from_h2(va.x, vb.x);
+    s[4 * k + 1] = c2_from_h2(va.y, vb.y);
+    s[4 * k + 2] = c2_from_h2(va.z, vb.z);
+    s[4 * k + 3] = c2_from_h2(va.w, vb.w);
+  }
+}
+
+// top half of (1 + S gamma_mu) psi (the tables of project<>)
+template <int MU, int S>
+__device__ __forceinline__ void project_pair(C2 (&h)[2][3], const C2 (&p)[12]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const C2 p0 = p[c], p1 = p[3 + c], p2 = p[6 + c], p3 = p[9 + c];
+    if constexpr (MU == 0) {
+      h[0][c] = S > 0 ? c2addi(p0, p3) : c2subi(p0, p3);
+      h[1][c] = S > 0 ? c2addi(p1, p2) : c2subi(p1, p2);
+    } else if constexpr (MU == 1) {
+      h[0][c] = S > 0 ? c2sub(p0, p3) : c2add(p0, p3);
+      h[1][c] = S > 0 ? c2add(p1, p2) : c2sub(p1, p2);
+    } else if constexpr (MU == 2) {
+      h[0][c] = S > 0 ? c2addi(p0, p2) : c2subi(p0, p2);
+      h[1][c] = S > 0 ? c2subi(p1, p3) : c2addi(p1, p3);
+    } else {
+      h[0][c] = S > 0 ? c2add(p0, p2) : c2sub(p0, p2);
+      h[1][c] = S > 0 ? c2add(p1, p3) : c2sub(p1, p3);
+    }
+  }
+}
+
+// sign * conj(a b - c d): the third link row from the first two
+__device__ __forceinline__ C2 conj_cross(C2 a, C2 b, C2 c, C2 d) {
+  const float2 p = __ffma2_rn(c.i, d.i, __fmul2_rn(a.r, b.r));
+  const float2 q = __ffma2_rn(a.i, b.i, __fmul2_rn(c.r, d.r));
+  const float2 s = __ffma2_rn(c.r, d.i, __fmul2_rn(c.i, d.r));
+  const float2 t = __ffma2_rn(a.r, b.i, __fmul2_rn(a.i, b.r));
+  return {fsub2(p, q), fsub2(s, t)};
+}
+
+template <int RECON, bool SIGN>
+__device__ __forceinline__ void load_link_pair(C2 (&u)[9], const void* base, int ja, int jb, int stride, float2 sign) {
+  constexpr int NC = RECON == 18 ? 9 : 6;
+  const uint2* p = reinterpret_cast<const uint2*>(base);
+#pragma unroll
+  for (int k = 0; k < (NC + 1) / 2; ++k) {
+    const uint2 va = ldg(p + (size_t)k * stride + ja);
+    const uint2 vb = ldg(p + (size_t)k * stride + jb);
+    u[2 * k] = c2_from_h2(va.x, vb.x);
+    if (2 * k + 1 < NC) u[2 * k + 1] = c2_from_h2(va.y, vb.y);
+  }
+  if constexpr (RECON == 12) {
+    u[6] = conj_cross(u[1], u[5], u[2], u[4]);
+    u[7] = conj_cross(u[2], u[3], u[0], u[5]);
+    u[8] = conj_cross(u[0], u[4], u[1], u[3]);
+    if constexpr (SIGN) {
+#pragma unroll
+      for (int k = 6; k < 9; ++k) u[k] = {__fmul2_rn(sign, u[k].r), __fmul2_rn(sign, u[k].i)};
+    }
+  }
+}
+
+// row r of U h (ADJ: of U^dag h) for one colour vector h
+template <bool ADJ>
+__device__ __forceinline__ C2 mv_row(const C2 (&u)[9], int r, const C2 (&h)[3]) {
+  const C2 e0 = ADJ ? u[r] : u[3 * r], e1 = ADJ ? u[3 + r] : u[3 * r + 1], e2 = ADJ ? u[6 + r] : u[3 * r + 2];
+  float2 a = __fmul2_rn(e0.r, h[0].r);
+  a = __ffma2_rn(e1.r, h[1].r, a);
+  a = __ffma2_rn(e2.r, h[2].r, a);
+  float2 b = __fmul2_rn(e0.i, h[0].i);
+  b = __ffma2_rn(e1.i, h[1].i, b);
+  b = __ffma2_rn(e2.i, h[2].i, b);
+  float2 c = __fmul2_rn(e0.r, h[0].i);
+  c = __ffma2_rn(e1.r, h[1].i, c);
+  c = __ffma2_rn(e2.r, h[2].i, c);
+  float2 d = __fmul2_rn(e0.i, h[0].r);
+  d = __ffma2_rn(e1.i, h[1].r, d);
+  d = __ffma2_rn(e2.i, h[2].r, d);
+  // U h: (a - b, c + d);  U^dag h: (a + b, c - d)
+  return ADJ ? C2{__fadd2_rn(a, b), fsub2(c, d)} : C2{fsub2(a, b), __fadd2_rn(c, d)};
+}
+
+// acc += K n v,  K = +1, -1, +i, -i (0, 1, 2, 3);  nn = -n
+template <int K>
+__device__ __forceinline__ void acc_scaled(C2& acc, C2 v, float2 n, float2 nn) {
+  if constexpr (K == 0) {
+    acc.r = __ffma2_rn(n, v.r, acc.r);
+    acc.i = __ffma2_rn(n, v.i, acc.i);
+  } else if constexpr (K == 1) {
+    acc.r = __ffma2_rn(nn, v.r, acc.r);
+    acc.i = __ffma2_rn(nn, v.i, acc.i);
+  } else if constexpr (K == 2) {
+    acc.r = __ffma2_rn(nn, v.i, acc.r);
+    acc.i = __ffma2_rn(n, v.r, acc.i);
+  } else {
+    acc.r = __ffma2_rn(n, v.i, acc.r);
+    acc.i = __ffma2_rn(nn, v.r, acc.i);
+  }
+}
+
+// uh = U h (or U^dag h) row by row, each row rebuilt into the four spins at once (the B tables
+// of reconstruct<>), scaled by the neighbours' site norms n
+template <int MU, int S, bool ADJ>
+__device__ __forceinline__ void mult_rebuild_pair(C2 (&acc)[12], const C2 (&u)[9], const C2 (&h)[2][3], float2 n) {
+  const float2 nn = make_float2(-n.x, -n.y);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const C2 a = mv_row<ADJ>(u, c, h[0]);
+    const C2 b = mv_row<ADJ>(u, c, h[1]);
+    acc_scaled<0>(acc[c], a, n, nn);
+    acc_scaled<0>(acc[3 + c], b, n, nn);
+    constexpr int P1 = S > 0 ? 0 : 1, M1 = S > 0 ? 1 : 0;  // +-1
+    constexpr int PI = S > 0 ? 2 : 3, MI = S > 0 ? 3 : 2;  // +-i
+    if constexpr (MU == 0) {
+      acc_scaled<MI>(acc[6 + c], b, n, nn);
+      acc_scaled<MI>(acc[9 + c], a, n, nn);
+    } else if constexpr (MU == 1) {
+      acc_scaled<P1>(acc[6 + c], b, n, nn);
+      acc_scaled<M1>(acc[9 + c], a, n, nn);
+    } else if constexpr (MU == 2) {
+      acc_scaled<MI>(acc[6 + c], a, n, nn);
+      acc_scaled<PI>(acc[9 + c], b, n, nn);
+    } else {
+      acc_scaled<P1>(acc[6 + c], a, n, nn);
+      acc_scaled<P1>(acc[9 + c], b, n, nn);
+    }
+  }
+}
+
+template <int RECON, int MU, bool DAG>
+__device__ __forceinline__ void hop_dir_pair(C2 (&acc)[12], const HopArgs& a, const Coord& ca, const Coord& cb,
+                                             int ia, int ib, const char* in, const float* in_norm) {
+  constexpr int SF = DAG ? +1 : -1;  // forward:  (1 - isign gamma)
+  constexpr int SB = DAG ? -1 : +1;  // backward: (1 + isign gamma)
+  const Geom& g = a.g;
+  const int last = g.L[MU] - 1;
+  C2 s[12], h[2][3], u[9];
+  {
+    Coord na = ca, nb = cb;
+    na.x[MU] = ca.x[MU] == last ? 0 : ca.x[MU] + 1;
+    nb.x[MU] = cb.x[MU] == last ? 0 : cb.x[MU] + 1;
+    const int ja = cb_index(g, na), jb = cb_index(g, nb);
+    load_spinor_pair(s, in, ja, jb, g.stride);
+    const float2 n = make_float2(ldg(in_norm + ja), ldg(in_norm + jb));
+    project_pair<MU, SF>(h, s);
+    const float ts = (float)g.t_sign;
+    const float2 sign = make_float2(ca.x[3] == g.L[3] - 1 ? ts : 1.f, cb.x[3] == g.L[3] - 1 ? ts : 1.f);
+    load_link_pair<RECON, MU == 3>(u, a.gauge_fwd[MU], ia, ib, g.stride, sign);
+    mult_rebuild_pair<MU, SF, false>(acc, u, h, n);
+  }
+  {
+    Coord na = ca, nb = cb;
+    na.x[MU] = ca.x[MU] == 0 ? last : ca.x[MU] - 1;
+    nb.x[MU] = cb.x[MU] == 0 ? last : cb.x[MU] - 1;
+    const int ja = cb_index(g, na), jb = cb_index(g, nb);
+    load_spinor_pair(s, in, ja, jb, g.stride);
+    const float2 n = make_float2(ldg(in_norm + ja), ldg(in_norm + jb));
+    project_pair<MU, SB>(h, s);
+    const float ts = (float)g.t_sign;
+    const float2 sign = make_float2(na.x[3] == g.L[3] - 1 ? ts : 1.f, nb.x[3] == g.L[3] - 1 ? ts : 1.f);
+    load_link_pair<RECON, MU == 3>(u, a.gauge_bwd[MU], ja, jb, g.stride, sign);
+    mult_rebuild_pair<MU, SB, true>(acc, u, h, n);
+  }
+}
+
+// Grid: Vh/2 / TX site blocks x nrhs, right-hand sides fastest (as hop_kernel with NRB = 1).
+template <int RECON, int MODE, bool DAG, bool REDUCE, int TX, int MINB>
+__global__ void __launch_bounds__(TX, MINB) hop_kernel_pair(const HopArgs a) {
+  const int sblock = blockIdx.x / a.nrhs;
+  const int rhs = blockIdx.x - sblock * a.nrhs;
+  const Geom& g = a.g;
+  const int half = g.Vh >> 1;
+  const int ia = sblock * TX + threadIdx.x;
+  double local = 0.0;
+  if (ia < half) {
+    const int ib = ia + half;
+    const Coord ca = cb_coords(g, ia, a.out_parity);
+    Coord cb = ca;
+    cb.x[3] = ca.x[3] + (g.L[3] >> 1);
+    cb.x[0] = (ca.x[0] & ~1) + ((a.out_parity + ca.x[1] + ca.x[2] + cb.x[3]) & 1);
+    const char* in = (const char*)a.in + (size_t)rhs * a.in_rhs_bytes;
+    const float* in_norm = a.in_norm + (size_t)rhs * a.norm_rhs_stride;
+    C2 acc[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) acc[k] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    hop_dir_pair<RECON, 0, DAG>(acc, a, ca, cb, ia, ib, in, in_norm);
+    hop_dir_pair<RECON, 1, DAG>(acc, a, ca, cb, ia, ib, in, in_norm);
+    hop_dir_pair<RECON, 2, DAG>(acc, a, ca, cb, ia, ib, in, in_norm);
+    hop_dir_pair<RECON, 3, DAG>(acc, a, ca, cb, ia, ib, in, in_norm);
+    cplx<float> sa[12], sb[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      sa[k] = {acc[k].r.x, acc[k].i.x};
+      sb[k] = {acc[k].r.y, acc[k].i.y};
+    }
+    local = (double)hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, ia, sa);
+    local += (double)hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, ib, sb);
+  }
+  if constexpr (REDUCE) {
+    __shared__ double wsum[TX / 32];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+#pragma unroll
+      for (int w = 0; w < TX / 32; ++w) s += wsum[w];
+      a.partials[(size_t)rhs * a.part_stride + sblock] = s;
     }
   }
 }

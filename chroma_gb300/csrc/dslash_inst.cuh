@@ -15,7 +15,7 @@ static int hop_shape(const HopArgs& a, HopShape sh, cudaStream_t s) {
     return nbx;
   };
 #define GBC_SHAPE(TX, NRB, MINB)                                 \
-  if (sh.tx == TX && sh.nrb == NRB && sh.minb == MINB) \
+  if (!sh.pair && sh.tx == TX && sh.nrb == NRB && sh.minb == MINB) \
     return go(hop_kernel<P, RECON, MODE, DAG, REDUCE, TX, NRB, MINB>, TX, NRB);
   GBC_SHAPE(128, 1, 1)
   GBC_SHAPE(128, 1, 6)
@@ -24,6 +24,21 @@ static int hop_shape(const HopArgs& a, HopShape sh, cudaStream_t s) {
   GBC_SHAPE(64, 2, 4)
   GBC_SHAPE(32, 12, 2)
 #undef GBC_SHAPE
+  if constexpr (std::is_same<P, PrecH>::value) {
+    // two sites per thread: blocks of TX threads cover 2 TX sites
+    if (!sh.pair || sh.nrb != 1 || (a.g.L[3] & 1)) return -1;
+    auto go2 = [&](auto kern, int tx) {
+      const int nbp = (a.g.Vh / 2 + tx - 1) / tx;
+      kern<<<(unsigned)(nbp * a.nrhs), tx, 0, s>>>(a);
+      return nbp;
+    };
+#define GBC_PAIR(TX, MINB) \
+  if (sh.tx == TX && sh.minb == MINB) return go2(hop_kernel_pair<RECON, MODE, DAG, REDUCE, TX, MINB>, TX);
+    GBC_PAIR(128, 2)
+    GBC_PAIR(128, 3)
+    GBC_PAIR(64, 6)
+#undef GBC_PAIR
+  }
   return -1;
 }
 
