@@ -50,6 +50,7 @@ def parse():
                     help="profiling mode: set up the workload and time one operator only")
     ap.add_argument("--nrhs", type=int, default=12)
     ap.add_argument("--recon", type=int, default=12, choices=[12, 18])
+    ap.add_argument("--no-extras", action="store_true", help="skip the smaller side workloads")
     ap.add_argument("--iters", type=int, default=3)
     return ap.parse_args()
 
@@ -183,6 +184,81 @@ def cpu_baseline(dims, links, chi_one, iters_full, nsrc, budget_s=20.0):
             "sample": f"{k} InvCG2 iterations of 1 of {nsrc} sources ({dt:.1f} s, oracle FP64, OpenMP); "
                       f"extrapolated x {iters_full} iterations x {nsrc} sources; operator setup {setup:.1f} s",
             "seconds_per_cg_iteration": per_iter}
+
+
+WEIGHTS = os.path.join(ROOT, "chroma_gb300", "weights", "cnn_16x16x16x32_k0.115_csw1.0.gbcw")
+
+
+def side_workloads(G):
+    """The smaller configurations, each reported beside the headline (not part of `value`):
+    - stout16: 16^3x32, eps 0.2 + 4 stout steps rho 0.1, kappa 0.12, c_sw 1.2, one Gaussian source:
+      mixed FP16/FP64 vs plain FP64 CG on the same GPU;
+    - uneven_batch: 8^3x16, 12^3x24, 16^3x32, 20^3x40 (kappa 0.124, c_sw 1.5, one Z2 source each)
+      solved as one batch (one multi-lattice stencil launch per application) vs one by one;
+    - learned16: 16^3x32, kappa 0.115, c_sw 1.0, FGMRES(16) with and without the trained network on
+      a gauge configuration outside its training set."""
+    from chroma_gb300 import sources as S
+    out = {}
+    # stout-smeared 16^3 x 32
+    dims = (16, 16, 16, 32)
+    u = G.gauge_synthetic(dims, 0.2, 4242, n_stout=4, rho=0.1, t_boundary=-1)
+    ctx = G.Context(dims, 1 / (2 * 0.12) - 4, 1.2, t_boundary=-1, max_rhs=1)
+    ctx.load_gauge(u)
+    chi = S.gaussian(dims, 17, cb=1).reshape(1, -1, 12)
+    rec = {}
+    for name, kw in (("mixed_fp16", dict(solver=G.SOLVER_MIXED)), ("plain_fp64_cg", dict(solver=G.SOLVER_CG))):
+        ctx.solve(chi, rsd_target=RSD, **kw)  # warm-up (tuning, workspaces)
+        ts = []
+        for _ in range(3):
+            _, res, rc = ctx.solve(chi, rsd_target=RSD, **kw)
+            ts.append(res[0]["device_seconds"])
+        rec[name] = {"seconds": statistics.median(ts), "iterations": res[0]["n_count"],
+                     "true_rel_resid": res[0]["rel_resid"]}
+    rec["speedup"] = rec["plain_fp64_cg"]["seconds"] / rec["mixed_fp16"]["seconds"]
+    out["stout16"] = rec
+    ctx.close()
+    # uneven lattices
+    lats = [(8, 8, 8, 16), (12, 12, 12, 24), (16, 16, 16, 32), (20, 20, 20, 40)]
+    mass = 1 / (2 * 0.124) - 4
+    ctxs, chis = [], []
+    for k, d in enumerate(lats):
+        c = G.Context(d, mass, 1.5, t_boundary=-1, max_rhs=1)
+        c.load_gauge(G.gauge_synthetic(d, 0.3, 7000 + k, t_boundary=-1))
+        ctxs.append(c)
+        chis.append(S.z2_noise(d, 8000 + k, cb=1).reshape(-1, 12))
+    batch = G.Batch(ctxs)
+    batch.solve(chis, rsd_target=RSD)
+    tb = []
+    for _ in range(3):
+        _, res = batch.solve(chis, rsd_target=RSD)
+        tb.append(res[0]["device_seconds"])
+    for c, x in zip(ctxs, chis):
+        c.solve(x.reshape(1, -1, 12), solver=G.SOLVER_MIXED, rsd_target=RSD)
+    ts = []
+    for _ in range(3):
+        tot = 0.0
+        for c, x in zip(ctxs, chis):
+            _, r1, _ = c.solve(x.reshape(1, -1, 12), solver=G.SOLVER_MIXED, rsd_target=RSD)
+            tot += r1[0]["device_seconds"]
+        ts.append(tot)
+    out["uneven_batch"] = {"lattices": ["x".join(map(str, d)) for d in lats],
+                           "batched_seconds": statistics.median(tb), "one_by_one_seconds": statistics.median(ts),
+                           "true_rel_resid_max": max(r["rel_resid"] for r in res),
+                           "iterations": [r["n_count"] for r in res]}
+    batch.close()
+    for c in ctxs:
+        c.close()
+    # learned preconditioner
+    if os.path.exists(WEIGHTS):
+        from chroma_gb300 import learn
+        dims = (16, 16, 16, 32)
+        ctx = G.Context(dims, 1 / (2 * 0.115) - 4, 1.0, t_boundary=-1, max_rhs=1)
+        ctx.load_gauge(G.gauge_synthetic(dims, 0.3, 999_999, t_boundary=-1))
+        ctx.load_precond(WEIGHTS)
+        learn.ablation(ctx, dims)  # warm-up
+        out["learned16"] = learn.ablation(ctx, dims)
+        ctx.close()
+    return out
 
 
 def run_reference(args, rank, world):
@@ -340,6 +416,7 @@ def main():
         # the cost of an InvCG2 iteration does not depend on the source: time it on odd-site noise
         cpu = cpu_baseline(dims, links, S.gaussian(dims, 1, cb=1).reshape(-1, 12), int(np.median(plain_iters)), nsrc)
 
+    extras = {} if args.no_extras else side_workloads(G)
     iters = [r["n_count"] for r in last]
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -362,6 +439,7 @@ def main():
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": nbytes},
         "gpu_launches": int(sum(r[0]["launches"] for r in results)),
         "clocks": clk,
+        "side_workloads": extras,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
