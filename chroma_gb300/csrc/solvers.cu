@@ -10,7 +10,8 @@
 //                           FP64 residual and solves for the correction with a CGNE whose operator
 //                           and search vectors are in the sloppy precision and whose residual is
 //                           refreshed from an FP32 operator (reliable updates)
-//   GBC_SOLVER_FGMRES       FGMRES(NKrylov), NDefl = 0 (fgmres.cu)
+//   GBC_SOLVER_FGMRES       FGMRES(NKrylov), NDefl = 0 (fgmres below), optionally preconditioned by
+//                           the learned network (precond.cu), inside the same FP64 defect correction
 //
 // Every right-hand side carries its own scalars on the device (CGScalars); a converged right-hand
 // side keeps alpha = beta = 0 so that the batch can run on until the last one converges.
