@@ -16,6 +16,7 @@ struct gbc_batch {
   cudaStream_t stream = nullptr;
   std::vector<cudaStream_t> saved;
   gbc::HopArgs* d_args = nullptr;  // [4][n]: (hop1, hop2) x (PLUS, MINUS)
+  gbc::LatCg* d_lat = nullptr;     // [n]: inner CG state per lattice
   int2* d_work = nullptr;
   int nwork = 0;
   std::string err;
@@ -76,7 +77,10 @@ int gbc_batch_create(gbc_batch** out, int n, gbc_ctx* const* ctxs) {
     b->ctx.push_back(ctxs[i]);
   }
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMalloc(&b->d_args, sizeof(HopArgs) * 4 * n) != cudaSuccess) {
+      cudaMalloc(&b->d_args, sizeof(HopArgs) * 4 * n) != cudaSuccess ||
+      cudaMalloc(&b->d_lat, sizeof(LatCg) * n) != cudaSuccess) {
+    if (b->d_args) cudaFree(b->d_args);
+    if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return GBC_ERR_CUDA;
   }
@@ -91,6 +95,8 @@ int gbc_batch_create(gbc_batch** out, int n, gbc_ctx* const* ctxs) {
   if (cudaMalloc(&b->d_work, sizeof(int2) * work.size()) != cudaSuccess ||
       cudaMemcpy(b->d_work, work.data(), sizeof(int2) * work.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
     cudaFree(b->d_args);
+    cudaFree(b->d_lat);
+    cudaStreamDestroy(b->stream);
     delete b;
     return GBC_ERR_CUDA;
   }
@@ -102,6 +108,7 @@ void gbc_batch_destroy(gbc_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->d_args) cudaFree(b->d_args);
+  if (b->d_lat) cudaFree(b->d_lat);
   if (b->d_work) cudaFree(b->d_work);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
@@ -197,26 +204,28 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
       if (hop_multi_launch(sloppy, recon, mode, dag, reduce, b->d_args + k * n, b->d_work, b->nwork, s) < 0)
         throw std::string("multi-lattice kernel variant not compiled");
       count_launch();
-      if (reduce)
-        for (int l = 0; l < n; ++l) {
-          gbc_ctx* c = b->ctx[l];
-          reduce_finalize(red(c), 1, 1, (c->g.Vh + 127) / 128, s);
-        }
     };
-    // one CGNE iteration for every lattice: M~ p (one launch per half), then M~^dag
+    // the inner CG state of every lattice, for the multi-lattice BLAS and scalar kernels; the
+    // stencil's |M~ p|^2 partials land in row 0 of each context's partials, the update's in row 1
+    std::vector<LatCg> lc(n);
+    for (int l = 0; l < n; ++l) {
+      gbc_ctx* c = b->ctx[l];
+      L& q = lat[l];
+      lc[l] = LatCg{c->g.Vh, (c->g.Vh + 127) / 128, q.es, q.r, q.pv, q.mmp, c->d_cg, c->d_partials,
+                    c->d_partials + c->part_stride};
+    }
+    GBC_CUDA(cudaMemcpyAsync(b->d_lat, lc.data(), sizeof(LatCg) * n, cudaMemcpyHostToDevice, s));
+    // one CGNE iteration for every lattice in 8 launches: M~ p (two stencil launches), alpha,
+    // M~^dag (two), the fused update with |r|^2, beta, p = r + b p
     auto body = [&]() {
       multi(0, HOP_CLOV, false, false);
       multi(1, HOP_XPAY, false, true);
-      for (int l = 0; l < n; ++l) cg_alpha(b->ctx[l]->d_cg, b->ctx[l]->d_result, b->ctx[l]->d_a, 1, s);
+      batch_cg_alpha(b->d_lat, n, s);
       multi(2, HOP_CLOV, true, false);
       multi(3, HOP_XPAY, true, false);
-      for (int l = 0; l < n; ++l) {
-        gbc_ctx* c = b->ctx[l];
-        L& q = lat[l];
-        blas_cg_update(c->g, c->d_a, q.es, q.pv, q.r, q.mmp, red(c), s);
-        cg_beta(c->d_cg, c->d_result, c->d_b, 1, s);
-        blas_xpay(c->g, q.r, c->d_b, q.pv, s);
-      }
+      batch_cg_update(pa, sloppy, b->d_lat, b->d_work, b->nwork, s);
+      batch_cg_beta(b->d_lat, n, s);
+      batch_xpay(pa, sloppy, b->d_lat, b->d_work, b->nwork, s);
     };
     int total = 0;
     for (int outer = 0; outer <= 50; ++outer) {

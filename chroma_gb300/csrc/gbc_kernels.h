@@ -169,6 +169,22 @@ void cg_alpha(CGScalars* st, const double* red_d, double* a_out, int nrhs, cudaS
 // after |r|^2 is in red_r: cp; converged -> active = 0; b = active ? cp/c : 0; c = cp; iters++
 void cg_beta(CGScalars* st, const double* red_r, double* b_out, int nrhs, cudaStream_t s);
 
+// One lattice of a batched CGNE (batch_kernels.cu): its inner vectors, scalars and partial sums.
+struct LatCg {
+  int Vh;
+  int nblk;                 // 128-site blocks = partials per sum
+  Spinor e, r;              // correction and residual (accumulator precision)
+  Spinor p, q;              // search vector and M~^dag M~ p (sloppy precision)
+  CGScalars* cg;
+  const double* hop_part;   // |M~ p|^2 per block, written by the stencil launch
+  double* upd_part;         // |r|^2 per block, written by batch_cg_update
+};
+// every lattice at once: one launch each (lat in device memory, work = the batch's work table)
+void batch_cg_alpha(const LatCg* lat, int n, cudaStream_t s);
+void batch_cg_update(int pa, int po, const LatCg* lat, const int2* work, int nwork, cudaStream_t s);
+void batch_cg_beta(const LatCg* lat, int n, cudaStream_t s);
+void batch_xpay(int pa, int po, const LatCg* lat, const int2* work, int nwork, cudaStream_t s);
+
 }  // namespace gbc
 
 namespace gbc {
