@@ -235,6 +235,73 @@ __device__ __forceinline__ void matvec_f2(float2 (&uh)[2][3], const cplx<float> 
   }
 }
 
+// fp16 storage: project the neighbour in half2 arithmetic straight from the stored words and
+// convert only the 6 projected colour components (12 conversions instead of 24). The sum of two
+// fp16 components is rounded once more to fp16, an error of the same size as their storage
+// rounding. Same tables as project<>.
+__device__ __forceinline__ __half2 as_h2(uint32_t w) { return *reinterpret_cast<__half2*>(&w); }
+__device__ __forceinline__ __half2 h2addi(__half2 a, __half2 b) {  // a + i b
+  return __hfma2(__lowhigh2highlow(b), __floats2half2_rn(-1.f, 1.f), a);
+}
+__device__ __forceinline__ __half2 h2subi(__half2 a, __half2 b) {  // a - i b
+  return __hfma2(__lowhigh2highlow(b), __floats2half2_rn(1.f, -1.f), a);
+}
+
+// colour c of the top half of (1 + S gamma_mu) psi from the stored fp16 words w
+template <int MU, int S>
+__device__ __forceinline__ void project_h2(const uint32_t (&w)[12], int c, __half2& a, __half2& b) {
+  const __half2 p0 = as_h2(w[c]), p1 = as_h2(w[3 + c]), p2 = as_h2(w[6 + c]), p3 = as_h2(w[9 + c]);
+  if constexpr (MU == 0) {
+    a = S > 0 ? h2addi(p0, p3) : h2subi(p0, p3);
+    b = S > 0 ? h2addi(p1, p2) : h2subi(p1, p2);
+  } else if constexpr (MU == 1) {
+    a = S > 0 ? __hsub2(p0, p3) : __hadd2(p0, p3);
+    b = S > 0 ? __hadd2(p1, p2) : __hsub2(p1, p2);
+  } else if constexpr (MU == 2) {
+    a = S > 0 ? h2addi(p0, p2) : h2subi(p0, p2);
+    b = S > 0 ? h2subi(p1, p3) : h2addi(p1, p3);
+  } else {
+    a = S > 0 ? __hadd2(p0, p2) : __hsub2(p0, p2);
+    b = S > 0 ? __hadd2(p1, p3) : __hsub2(p1, p3);
+  }
+}
+
+template <int MU, int S>
+__device__ __forceinline__ void load_project_h(float2 (&h)[2][3], float& n, const void* base, const float* norm,
+                                               int idx, int stride) {
+  const uint4* p = reinterpret_cast<const uint4*>(base);
+  uint32_t w[12];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const uint4 v = ldg(p + (size_t)k * stride + idx);
+    w[4 * k] = v.x;
+    w[4 * k + 1] = v.y;
+    w[4 * k + 2] = v.z;
+    w[4 * k + 3] = v.w;
+  }
+  n = ldg(norm + idx);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    __half2 a, b;
+    project_h2<MU, S>(w, c, a, b);
+    h[0][c] = __half22float2(a);
+    h[1][c] = __half22float2(b);
+  }
+}
+
+// load the neighbour and project it: half2 projection for fp16 storage, FP32 otherwise
+template <typename P, int MU, int S>
+__device__ __forceinline__ void load_project(float2 (&h)[2][3], float& n, const void* base, const float* norm, int idx,
+                                             int stride) {
+  if constexpr (std::is_same<P, PrecH>::value) {
+    load_project_h<MU, S>(h, n, base, norm, idx, stride);
+  } else {
+    float2 s[12];
+    load_spinor_f2<P>(s, n, base, norm, idx, stride);
+    project_f2<MU, S>(h, s);
+  }
+}
+
 // fp16 spinors are stored divided by their site norm: scale the projected half spinor back
 template <typename P>
 __device__ __forceinline__ void scale_f2(float2 (&h)[2][3], float n) {
@@ -253,15 +320,14 @@ __device__ __forceinline__ void hop_dir_f2(float2 (&acc)[12], const HopArgs& a, 
   constexpr int SF = DAG ? +1 : -1;
   constexpr int SB = DAG ? -1 : +1;
   const Geom& g = a.g;
-  float2 s[12], h[2][3], uh[2][3];
+  float2 h[2][3], uh[2][3];
   cplx<float> u[9];
   float n;
   {
     Coord nb = c;
     nb.x[MU] = c.x[MU] + 1 == g.L[MU] ? 0 : c.x[MU] + 1;
     const int ni = cb_index(g, nb);
-    load_spinor_f2<P>(s, n, in, in_norm, ni, g.stride);
-    project_f2<MU, SF>(h, s);
+    load_project<P, MU, SF>(h, n, in, in_norm, ni, g.stride);
     scale_f2<P>(h, n);
     const float sign = (MU == 3 && c.x[3] == g.L[3] - 1) ? (float)g.t_sign : 1.0f;
     load_link<P, RECON>(u, a.gauge_fwd[MU], idx, g.stride, sign);
@@ -272,8 +338,7 @@ __device__ __forceinline__ void hop_dir_f2(float2 (&acc)[12], const HopArgs& a, 
     Coord nb = c;
     nb.x[MU] = c.x[MU] == 0 ? g.L[MU] - 1 : c.x[MU] - 1;
     const int ni = cb_index(g, nb);
-    load_spinor_f2<P>(s, n, in, in_norm, ni, g.stride);
-    project_f2<MU, SB>(h, s);
+    load_project<P, MU, SB>(h, n, in, in_norm, ni, g.stride);
     scale_f2<P>(h, n);
     const float sign = (MU == 3 && nb.x[3] == g.L[3] - 1) ? (float)g.t_sign : 1.0f;
     load_link<P, RECON>(u, a.gauge_bwd[MU], ni, g.stride, sign);
@@ -346,13 +411,12 @@ __device__ __forceinline__ void hop_dir_sm(float2 (&acc)[12], const float4 (*lsm
   constexpr int SF = DAG ? +1 : -1;
   constexpr int SB = DAG ? -1 : +1;
   const Geom& g = a.g;
-  float2 sp[12], h[2][3], uh[2][3];
+  float2 h[2][3], uh[2][3];
   float n;
   {
     Coord nb = c;
     nb.x[MU] = c.x[MU] + 1 == g.L[MU] ? 0 : c.x[MU] + 1;
-    load_spinor_f2<P>(sp, n, in, in_norm, cb_index(g, nb), g.stride);
-    project_f2<MU, SF>(h, sp);
+    load_project<P, MU, SF>(h, n, in, in_norm, cb_index(g, nb), g.stride);
     scale_f2<P>(h, n);
     matvec_sm<TX>(uh, lsm, 2 * MU, s, h);
     reconstruct_f2<MU, SF>(acc, uh);
@@ -360,8 +424,7 @@ __device__ __forceinline__ void hop_dir_sm(float2 (&acc)[12], const float4 (*lsm
   {
     Coord nb = c;
     nb.x[MU] = c.x[MU] == 0 ? g.L[MU] - 1 : c.x[MU] - 1;
-    load_spinor_f2<P>(sp, n, in, in_norm, cb_index(g, nb), g.stride);
-    project_f2<MU, SB>(h, sp);
+    load_project<P, MU, SB>(h, n, in, in_norm, cb_index(g, nb), g.stride);
     scale_f2<P>(h, n);
     matvec_sm<TX>(uh, lsm, 2 * MU + 1, s, h);
     reconstruct_f2<MU, SB>(acc, uh);
@@ -546,44 +609,26 @@ __device__ __forceinline__ C2 c2_from_h2(uint32_t wa, uint32_t wb) {
   return C2{make_float2(__low2float(ha), __low2float(hb)), make_float2(__high2float(ha), __high2float(hb))};
 }
 
-__device__ __forceinline__ C2 c2add(C2 a, C2 b) { return {__fadd2_rn(a.r, b.r), __fadd2_rn(a.i, b.i)}; }
-__device__ __forceinline__ C2 c2sub(C2 a, C2 b) { return {fsub2(a.r, b.r), fsub2(a.i, b.i)}; }
-__device__ __forceinline__ C2 c2addi(C2 a, C2 b) { return {fsub2(a.r, b.i), __fadd2_rn(a.i, b.r)}; }  // a + i b
-__device__ __forceinline__ C2 c2subi(C2 a, C2 b) { return {__fadd2_rn(a.r, b.i), fsub2(a.i, b.r)}; }  // a - i b
-
-// the 12 components of the fp16 spinor at cb sites ja, jb (still divided by their site norms)
-__device__ __forceinline__ void load_spinor_pair(C2 (&s)[12], const void* base, int ja, int jb, int stride) {
+// project the fp16 neighbours of both sites in half2 arithmetic (as load_project_h), then convert
+// the projected components into the pair registers
+template <int MU, int S>
+__device__ __forceinline__ void load_project_pair(C2 (&h)[2][3], const void* base, int ja, int jb, int stride) {
   const uint4* p = reinterpret_cast<const uint4*>(base);
+  uint32_t wa[12], wb[12];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const uint4 va = ldg(p + (size_t)k * stride + ja);
     const uint4 vb = ldg(p + (size_t)k * stride + jb);
-    s[4 * k + 0] = c2_from_h2(va.x, vb.x);
-    s[4 * k + 1] = c2_from_h2(va.y, vb.y);
-    s[4 * k + 2] = c2_from_h2(va.z, vb.z);
-    s[4 * k + 3] = c2_from_h2(va.w, vb.w);
+    wa[4 * k] = va.x; wa[4 * k + 1] = va.y; wa[4 * k + 2] = va.z; wa[4 * k + 3] = va.w;
+    wb[4 * k] = vb.x; wb[4 * k + 1] = vb.y; wb[4 * k + 2] = vb.z; wb[4 * k + 3] = vb.w;
   }
-}
-
-// top half of (1 + S gamma_mu) psi (the tables of project<>)
-template <int MU, int S>
-__device__ __forceinline__ void project_pair(C2 (&h)[2][3], const C2 (&p)[12]) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const C2 p0 = p[c], p1 = p[3 + c], p2 = p[6 + c], p3 = p[9 + c];
-    if constexpr (MU == 0) {
-      h[0][c] = S > 0 ? c2addi(p0, p3) : c2subi(p0, p3);
-      h[1][c] = S > 0 ? c2addi(p1, p2) : c2subi(p1, p2);
-    } else if constexpr (MU == 1) {
-      h[0][c] = S > 0 ? c2sub(p0, p3) : c2add(p0, p3);
-      h[1][c] = S > 0 ? c2add(p1, p2) : c2sub(p1, p2);
-    } else if constexpr (MU == 2) {
-      h[0][c] = S > 0 ? c2addi(p0, p2) : c2subi(p0, p2);
-      h[1][c] = S > 0 ? c2subi(p1, p3) : c2addi(p1, p3);
-    } else {
-      h[0][c] = S > 0 ? c2add(p0, p2) : c2sub(p0, p2);
-      h[1][c] = S > 0 ? c2add(p1, p3) : c2sub(p1, p3);
-    }
+    __half2 aa, ba, ab, bb;
+    project_h2<MU, S>(wa, c, aa, ba);
+    project_h2<MU, S>(wb, c, ab, bb);
+    h[0][c] = C2{make_float2(__low2float(aa), __low2float(ab)), make_float2(__high2float(aa), __high2float(ab))};
+    h[1][c] = C2{make_float2(__low2float(ba), __low2float(bb)), make_float2(__high2float(ba), __high2float(bb))};
   }
 }
 
@@ -692,15 +737,14 @@ __device__ __forceinline__ void hop_dir_pair(C2 (&acc)[12], const HopArgs& a, co
   constexpr int SB = DAG ? -1 : +1;  // backward: (1 + isign gamma)
   const Geom& g = a.g;
   const int last = g.L[MU] - 1;
-  C2 s[12], h[2][3], u[9];
+  C2 h[2][3], u[9];
   {
     Coord na = ca, nb = cb;
     na.x[MU] = ca.x[MU] == last ? 0 : ca.x[MU] + 1;
     nb.x[MU] = cb.x[MU] == last ? 0 : cb.x[MU] + 1;
     const int ja = cb_index(g, na), jb = cb_index(g, nb);
-    load_spinor_pair(s, in, ja, jb, g.stride);
+    load_project_pair<MU, SF>(h, in, ja, jb, g.stride);
     const float2 n = make_float2(ldg(in_norm + ja), ldg(in_norm + jb));
-    project_pair<MU, SF>(h, s);
     const float ts = (float)g.t_sign;
     const float2 sign = make_float2(ca.x[3] == g.L[3] - 1 ? ts : 1.f, cb.x[3] == g.L[3] - 1 ? ts : 1.f);
     load_link_pair<RECON, MU == 3>(u, a.gauge_fwd[MU], ia, ib, g.stride, sign);
@@ -711,9 +755,8 @@ __device__ __forceinline__ void hop_dir_pair(C2 (&acc)[12], const HopArgs& a, co
     na.x[MU] = ca.x[MU] == 0 ? last : ca.x[MU] - 1;
     nb.x[MU] = cb.x[MU] == 0 ? last : cb.x[MU] - 1;
     const int ja = cb_index(g, na), jb = cb_index(g, nb);
-    load_spinor_pair(s, in, ja, jb, g.stride);
+    load_project_pair<MU, SB>(h, in, ja, jb, g.stride);
     const float2 n = make_float2(ldg(in_norm + ja), ldg(in_norm + jb));
-    project_pair<MU, SB>(h, s);
     const float ts = (float)g.t_sign;
     const float2 sign = make_float2(na.x[3] == g.L[3] - 1 ? ts : 1.f, nb.x[3] == g.L[3] - 1 ? ts : 1.f);
     load_link_pair<RECON, MU == 3>(u, a.gauge_bwd[MU], ja, jb, g.stride, sign);
