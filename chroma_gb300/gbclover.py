@@ -29,7 +29,8 @@ EXPORTS = ["gbc_create", "gbc_destroy", "gbc_strerror", "gbc_last_error", "gbc_l
            "gbc_gauge_synthetic", "gbc_time_operator", "gbc_tune_report", "gbc_apply_meo_noalloc",
            "gbc_precond_init", "gbc_precond_save", "gbc_precond_weights", "gbc_precond_set_weights",
            "gbc_precond_apply", "gbc_precond_loss_grad", "gbc_precond_train", "gbc_batch_create",
-           "gbc_batch_destroy", "gbc_batch_solve", "gbc_batch_last_error"]
+           "gbc_batch_destroy", "gbc_batch_solve", "gbc_batch_last_error", "gbc_stout_smear",
+           "gbc_solve_multishift"]
 
 
 class Geom(C.Structure):
@@ -110,6 +111,9 @@ def load(path=LIB_PATH):
                                     C.POINTER(Result)]
     lib.gbc_batch_last_error.restype = C.c_char_p
     lib.gbc_batch_last_error.argtypes = [C.c_void_p]
+    lib.gbc_stout_smear.argtypes = [C.POINTER(Geom), C.c_int, C.c_double, C.POINTER(C.c_int), dp, dp]
+    lib.gbc_solve_multishift.argtypes = [C.c_void_p, C.POINTER(SolveParams), C.c_int, dp, dp, C.POINTER(dp), dp,
+                                         C.POINTER(Result)]
     _lib = lib
     return lib
 
@@ -137,6 +141,19 @@ def gauge_synthetic(dims, eps, seed, n_stout=0, rho=0.0, smear_dirs=(1, 1, 1, 1)
                                  _dp(u.view(np.float64)))
     if rc != GBC_OK:
         raise GBCError(rc, "gauge_synthetic")
+    return u
+
+
+def stout_smear(dims, links, n_steps, rho, smear_dirs=(1, 1, 1, 1)):
+    """n_steps stout steps of weight rho on the GPU (FP64); links (V, 4, 3, 3) complex128, no BC."""
+    lib = load()
+    u = np.ascontiguousarray(links, dtype=np.complex128).copy()
+    g = Geom((C.c_int * 4)(*dims), 1)
+    sd = (C.c_int * 4)(*smear_dirs)
+    rc = lib.gbc_stout_smear(C.byref(g), int(n_steps), float(rho), sd, _dp(u.view(np.float64)),
+                             _dp(u.view(np.float64)))
+    if rc != GBC_OK:
+        raise GBCError(rc, "stout_smear")
     return u
 
 
@@ -220,6 +237,23 @@ class Context:
         rc = self.lib.gbc_solve(self.h, C.byref(p), nrhs, _dp(psi.view(np.float64)), _dp(chi.view(np.float64)), res)
         if rc != GBC_OK and raise_on_error:
             self._check(rc, "solve")
+        return psi, [r.as_dict() for r in res], rc
+
+    def solve_multishift(self, chi, shifts, rsd_target=1e-10, rsd_targets=None, max_iter=10000, tol_factor=10.0,
+                         raise_on_error=True):
+        """(M~^dag M~ + shift_s) psi_s = chi for every shift (odd sites); returns psi (ns, V, 12)."""
+        chi = np.ascontiguousarray(chi, dtype=np.complex128).reshape(self.V, 12)
+        ns = len(shifts)
+        psi = np.zeros((ns, self.V, 12), dtype=np.complex128)
+        sh = (C.c_double * ns)(*[float(x) for x in shifts])
+        rt = None if rsd_targets is None else (C.c_double * ns)(*[float(x) for x in rsd_targets])
+        pp = (C.POINTER(C.c_double) * ns)(*[_dp(psi[k].view(np.float64)) for k in range(ns)])
+        p = SolveParams(SOLVER_CG, SYS_MDAGM, float(rsd_target), int(max_iter), 0.1, float(tol_factor), 0, 0.0, 0,
+                        16, 0, 1)
+        res = (Result * ns)()
+        rc = self.lib.gbc_solve_multishift(self.h, C.byref(p), ns, sh, rt, pp, _dp(chi.view(np.float64)), res)
+        if rc != GBC_OK and raise_on_error:
+            self._check(rc, "solve_multishift")
         return psi, [r.as_dict() for r in res], rc
 
     def solve_device(self, psi_ptr, chi_ptr, nrhs, solver=SOLVER_CG, system=SYS_MEO, rsd_target=1e-10,

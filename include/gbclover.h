@@ -243,6 +243,28 @@ int gbc_precond_train(gbc_ctx* ctx, int nsamples, const double* in, const double
 int gbc_gauge_synthetic(const int dims[4], double eps, unsigned long long seed, int n_stout, double rho,
                         const int smear_dirs[4], int t_boundary, double* links);
 
+/* ---- multi-shift solves (RHMC) --------------------------------------------------------------- */
+/* (M~^dag M~ + shifts[s]) psi[s] = chi on the odd sites for s = 0..nshift-1 in one Krylov space:
+   replaces MdagMMultiSysSolverCG::operator()(psi, shifts, chi)
+   (lib/actions/ferm/invert/multi_syssolver_mdagm_cg.h:58-80) and its MInvCG2
+   (lib/actions/ferm/invert/minvcg2.cc:70-357), same recursion and stopping rule, FP64.
+   shifts[s] >= 0; rsd_targets[s] is RsdCG per shift (NULL: p->rsd_target for all); p->max_iter
+   and p->rsd_tolerance_factor are used, the other fields of p are ignored.  chi and every psi[s]
+   are canonical host arrays (only their odd sites are read / written); res[s] per shift, with the
+   FP64 true relative residual of that shifted system. */
+int gbc_solve_multishift(gbc_ctx* ctx, const gbc_solve_params* p, int nshift, const double* shifts,
+                         const double* rsd_targets, double* const* psi, const double* chi, gbc_result* res);
+
+/* ---- gauge-field setup on the device ------------------------------------------------------- */
+/* n_steps stout-smearing steps of weight rho in the directions with smear_dirs[mu] != 0 (NULL =
+   all four), on the GPU in FP64: replaces smear_links / StoutFermState::create
+   (lib/util/gauge/stout_utils.cc:936-966, lib/actions/ferm/fermstates/stout_fermstate_w.h:137-176)
+   for a solver's setup.  links_in and links_out are host arrays in the canonical layout of
+   gbc_load_gauge (they may be the same array); geom->t_boundary is not applied (Chroma applies
+   the fermion boundary after smearing).  Allocates two link fields on the device for the call. */
+int gbc_stout_smear(const gbc_geom* geom, int n_steps, double rho, const int smear_dirs[4], const double* links_in,
+                    double* links_out);
+
 #ifdef __cplusplus
 }
 #endif
