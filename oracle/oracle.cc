@@ -433,7 +433,7 @@ struct Op {
   const Geom* g;
   std::vector<std::complex<R>> u;     // dslash links
   std::vector<CloverSite<R>> clov;     // A on all sites
-  std::vector<CloverSite<R>> invclov;  // A^-1 on even sites
+  std::vector<CloverSite<R>> invclov;  // A^-1 on all sites (the odd ones serve the symmetric operator)
   bool twisted = false;
   R twisted_m = 0;
   double logdet_even = 0;
@@ -528,6 +528,43 @@ static void eo_op(const Op<R>& op, std::complex<R>* chi, const std::complex<R>* 
     for (int k = 0; k < NSP; ++k) chi[s * NSP + k] += (R)(-0.25) * t1[s * NSP + k];
     if (op.twisted) {
       // gamma_5 = diag(1,1,-1,-1) in this basis; verified against GAMMA5 at init
+      for (int a = 0; a < Ns; ++a) {
+        R g5 = (R)GAMMA5[a][a].real();
+        for (int c = 0; c < Nc; ++c) {
+          std::complex<R> v = psi[s * NSP + a * Nc + c] * std::complex<R>(0, g5 * op.twisted_m);
+          chi[s * NSP + a * Nc + c] += (R)isign * v;
+        }
+      }
+    }
+  }
+}
+
+// Symmetric even-odd preconditioned operator (seoprec_clover_linop_w.cc:145-187):
+//   PLUS:  chi_o = psi_o - 1/4 A_oo^-1 D_oe A_ee^-1 D_eo psi_o
+//   MINUS: chi_o = psi_o - 1/4 D_oe^dag A_ee^-1 D_eo^dag A_oo^-1 psi_o   (its adjoint)
+// (+ isign * i mu gamma_5 psi_o when twisted).  A_oo^-1 M~ = this operator for PLUS.
+template <typename R>
+static void sym_op(const Op<R>& op, std::complex<R>* chi, const std::complex<R>* psi, int isign) {
+  const Geom& g = *op.g;
+  std::vector<std::complex<R>> t1(g.V * NSP), t2(g.V * NSP);
+  if (isign > 0) {
+    dslash(op, t1.data(), psi, isign, 0);
+    clover_apply(op, op.invclov, t2.data(), t1.data(), 0);
+    dslash(op, t1.data(), t2.data(), isign, 1);
+    clover_apply(op, op.invclov, t2.data(), t1.data(), 1);
+  } else {
+    clover_apply(op, op.invclov, t1.data(), psi, 1);
+    dslash(op, t2.data(), t1.data(), isign, 0);
+    clover_apply(op, op.invclov, t1.data(), t2.data(), 0);
+    dslash(op, t2.data(), t1.data(), isign, 1);
+  }
+  const auto& sites = g.sites[1];
+  const long n = (long)sites.size();
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < n; ++i) {
+    long s = sites[i];
+    for (int k = 0; k < NSP; ++k) chi[s * NSP + k] = psi[s * NSP + k] + (R)(-0.25) * t2[s * NSP + k];
+    if (op.twisted) {
       for (int a = 0; a < Ns; ++a) {
         R g5 = (R)GAMMA5[a][a].real();
         for (int c = 0; c < Nc; ++c) {
@@ -985,6 +1022,9 @@ orc_ctx* orc_create(const int* dims, const double* links, double mass, double cs
   for (long s : g.sites[0]) ldl_invert_site(op.invclov[s], ld, nneg);
   op.logdet_even = ld;
   op.nneg = nneg;
+  double ld_odd = 0;
+  int nneg_odd = 0;
+  for (long s : g.sites[1]) ldl_invert_site(op.invclov[s], ld_odd, nneg_odd);
   op.twisted = twisted != 0;
   op.twisted_m = twisted_m;
   // single-precision copy for the reliable CG inner operator
@@ -1020,7 +1060,7 @@ long orc_volume(orc_ctx* c) { return c->g->V; }
 double orc_logdet_even(orc_ctx* c) { return c->op->logdet_even; }
 int orc_neg_eigs(orc_ctx* c) { return c->op->nneg; }
 
-// Packed clover (72 doubles/site) of A on all sites, and of A^-1 on the even sites.
+// Packed clover (72 doubles/site) of A and of A^-1, all sites.
 void orc_get_clover(orc_ctx* c, double* clov, double* invclov) {
   std::memcpy(clov, c->op->clov.data(), sizeof(CloverSite<double>) * c->g->V);
   std::memcpy(invclov, c->op->invclov.data(), sizeof(CloverSite<double>) * c->g->V);
@@ -1036,7 +1076,8 @@ double orc_clover_invert_packed(long nsites, double* packed) {
 }
 
 // op codes shared with the C-ABI: 0 D (hopping term, output parity cb), 1 A (clover, parity cb),
-// 2 A^-1 (even parity only), 3 M~ (odd), 4 M~^dag M~ (odd), 5 unpreconditioned M (full)
+// 2 A^-1 (parity cb), 3 M~ (odd), 4 M~^dag M~ (odd), 5 unpreconditioned M (full),
+// 6 symmetric M_s (odd), 7 M_s^dag M_s (odd)
 int orc_apply(orc_ctx* c, int opcode, int isign, int cb, double* out, const double* in) {
   cd* o = reinterpret_cast<cd*>(out);
   const cd* i = reinterpret_cast<const cd*>(in);
@@ -1044,7 +1085,7 @@ int orc_apply(orc_ctx* c, int opcode, int isign, int cb, double* out, const doub
   switch (opcode) {
     case 0: dslash(op, o, i, isign, cb); return 0;
     case 1: clover_apply(op, op.clov, o, i, cb); return 0;
-    case 2: if (cb != 0) return -1; clover_apply(op, op.invclov, o, i, 0); return 0;
+    case 2: clover_apply(op, op.invclov, o, i, cb); return 0;
     case 3: eo_op(op, o, i, isign); return 0;
     case 4: {
       std::vector<cd> t(c->g->V * NSP);
@@ -1053,6 +1094,13 @@ int orc_apply(orc_ctx* c, int opcode, int isign, int cb, double* out, const doub
       return 0;
     }
     case 5: unprec_op(op, o, i, isign); return 0;
+    case 6: sym_op(op, o, i, isign); return 0;
+    case 7: {
+      std::vector<cd> t(c->g->V * NSP);
+      sym_op(op, t.data(), i, +1);
+      sym_op(op, o, t.data(), -1);
+      return 0;
+    }
   }
   return -1;
 }
@@ -1065,8 +1113,9 @@ int orc_apply_f32(orc_ctx* c, int opcode, int isign, int cb, float* out, const f
   switch (opcode) {
     case 0: dslash(op, o, i, isign, cb); return 0;
     case 1: clover_apply(op, op.clov, o, i, cb); return 0;
-    case 2: if (cb != 0) return -1; clover_apply(op, op.invclov, o, i, 0); return 0;
+    case 2: clover_apply(op, op.invclov, o, i, cb); return 0;
     case 3: eo_op(op, o, i, isign); return 0;
+    case 6: sym_op(op, o, i, isign); return 0;
   }
   return -1;
 }

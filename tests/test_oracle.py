@@ -243,6 +243,30 @@ def test_schur_complement_identity(orc):
     assert np.abs(full[par == 1] - meo[par == 1]).max() < 1e-12
 
 
+def test_symmetric_operator_identities(orc):
+    """The symmetric operator M_s = 1 - 1/4 A_oo^-1 D_oe A_ee^-1 D_eo (seoprec_clover_linop_w.cc:
+    145-187) is A_oo^-1 M~; its MINUS application is its adjoint; A_oo A_oo^-1 = 1 on the odd
+    sites; OP_SYM_MDAGM = M_s^dag M_s."""
+    dims = (4, 4, 4, 8)
+    u = orc.apply_bc(dims, orc.gauge_hot(dims, 0.3, 43))
+    op = OracleOp(dims, u, 1 / (2 * 0.12) - 4, 1.3)
+    x = rand_spinor(dims, 8, cb=1)
+    y = rand_spinor(dims, 9, cb=1)
+    par = parity(dims)
+    ms = op.apply(O.OP_SYM, x, +1, 1)
+    want = op.apply(O.OP_CLOVER_INV, op.apply(O.OP_MEO, x), +1, 1)
+    assert np.abs(ms[par == 1] - want[par == 1]).max() < 1e-12 * np.abs(want).max()
+    back = op.apply(O.OP_CLOVER, op.apply(O.OP_CLOVER_INV, x, +1, 1), +1, 1)
+    assert np.abs(back[par == 1] - x[par == 1]).max() < 1e-12
+    msd = op.apply(O.OP_SYM, y, -1, 1)
+    lhs = op.inner(y, ms)
+    rhs = op.inner(msd, x)
+    assert abs(lhs - rhs) < 1e-12 * abs(lhs)
+    mm = op.apply(O.OP_SYM_MDAGM, x, +1, 1)
+    want = op.apply(O.OP_SYM, ms, -1, 1)
+    assert np.abs(mm[par == 1] - want[par == 1]).max() < 1e-12 * np.abs(want).max()
+
+
 @pytest.mark.parametrize("solver", [O.SOLVER_CG, O.SOLVER_RELIABLE_CG, O.SOLVER_FGMRES])
 def test_solvers_converge(orc, solver):
     dims = (4, 4, 4, 8)
