@@ -203,7 +203,7 @@ __global__ void clover_build_kernel(Dims D, const double2* canon, CloverCoeffs c
     }
   double* io = inv + s * 72;
   const int par = (x[0] + x[1] + x[2] + x[3]) & 1;
-  if (par != inv_parity) {
+  if (inv_parity != 2 && par != inv_parity) {
     for (int i = 0; i < 72; ++i) io[i] = 0.0;
     logdet[s] = 0.0;
     nneg[s] = 0;
@@ -257,8 +257,45 @@ void clover_build(const int dims[4], const double* canon_links, const CloverCoef
                                                                clov, inv, logdet, nneg, inv_parity, V);
 }
 
+// inv = A^-1 on the sites of parity `parity` (clov on all sites, canonical site order)
+__global__ void clover_invert_parity_kernel(Dims D, const double* clov, double* inv, int parity, long V) {
+  const long s = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (s >= V) return;
+  long r = s;
+  int sum = 0;
+  for (int k = 0; k < 4; ++k) {
+    sum += (int)(r % D.L[k]);
+    r /= D.L[k];
+  }
+  if ((sum & 1) != parity) return;
+  const double* p = clov + s * 72;
+  double* q = inv + s * 72;
+  double d[2][6];
+  cplx<double> o[2][15];
+  for (int b = 0; b < 2; ++b) {
+    for (int i = 0; i < 6; ++i) d[b][i] = p[6 * b + i];
+    for (int i = 0; i < 15; ++i) o[b][i] = {p[12 + 30 * b + 2 * i], p[13 + 30 * b + 2 * i]};
+  }
+  double ld = 0.0;
+  int nn = 0;
+  for (int b = 0; b < 2; ++b) ldl_invert_block(d[b], o[b], ld, nn);
+  for (int b = 0; b < 2; ++b) {
+    for (int i = 0; i < 6; ++i) q[6 * b + i] = d[b][i];
+    for (int i = 0; i < 15; ++i) {
+      q[12 + 30 * b + 2 * i] = o[b][i].re;
+      q[13 + 30 * b + 2 * i] = o[b][i].im;
+    }
+  }
+}
+
 void clover_invert(long nsites, double* packed, double* logdet, int* nneg, cudaStream_t s) {
   clover_invert_kernel<<<(unsigned)((nsites + 63) / 64), 64, 0, s>>>(nsites, packed, logdet, nneg);
+}
+
+void clover_invert_parity(const int dims[4], const double* clov, double* inv, int parity, cudaStream_t s) {
+  Dims D{{dims[0], dims[1], dims[2], dims[3]}};
+  long V = (long)dims[0] * dims[1] * dims[2] * dims[3];
+  clover_invert_parity_kernel<<<(unsigned)((V + 63) / 64), 64, 0, s>>>(D, clov, inv, parity, V);
 }
 
 }  // namespace gbc

@@ -90,6 +90,7 @@ static void free_prec(PrecFields& f) {
   for (int p = 0; p < 2; ++p)
     if (f.clov[p]) cudaFree(f.clov[p]);
   if (f.clovinv) cudaFree(f.clovinv);
+  if (f.clovinv_odd) cudaFree(f.clovinv_odd);
   f = PrecFields{};
 }
 
@@ -253,6 +254,7 @@ void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, con
 }
 
 void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, bool reduce) {
+  if (c->sym) return apply_seo(c, prec, dag, in, out, tmp_e, reduce);
   const PrecFields& f = c->pf[pidx(prec)];
   // t_e = A_ee^-1 D_eo in_o ;  out_o = A_oo in_o - 1/4 D_oe t_e  (+ isign i mu gamma_5 in_o)
   hop(c, prec, 0, HOP_CLOV, dag, 1.0, in, tmp_e, nullptr, f.clovinv, false);
@@ -260,9 +262,41 @@ void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& o
 }
 
 void apply_clover(gbc_ctx* c, int prec, int parity, bool inverse, const Spinor& in, const Spinor& out) {
+  if (inverse && parity == 1) ensure_sym(c, prec);
   const PrecFields& f = c->pf[pidx(prec)];
-  blas_clover(c->g, inverse ? f.clovinv : f.clov[parity], out, in, c->stream);
+  blas_clover(c->g, inverse ? (parity == 0 ? f.clovinv : f.clovinv_odd) : f.clov[parity], out, in, c->stream);
   GBC_CUDA(cudaGetLastError());
+}
+
+void ensure_sym(gbc_ctx* c, int prec) {
+  ensure_prec(c, prec);
+  PrecFields& f = c->pf[pidx(prec)];
+  if (f.clovinv_odd) return;
+  GBC_CUDA(cudaMalloc(&f.clovinv_odd, clover_bytes(prec) * c->g.stride));
+  void* planes[2] = {nullptr, f.clovinv_odd};
+  pack_clover(c->g, c->d_inv, prec, planes, 2, c->stream);
+  GBC_CUDA(cudaGetLastError());
+}
+
+// Symmetric even-odd operator (seoprec_clover_linop_w.cc:145-187):
+//   PLUS   out = in - 1/4 A_oo^-1 D_oe A_ee^-1 D_eo in     (t_e, then the clover-inverse epilogue)
+//   MINUS  out = in - 1/4 D_oe^dag A_ee^-1 D_eo^dag A_oo^-1 in
+// The last step leaves 1/4 (...) in out and blas_xmy_norm2 turns it into in - out with |out|^2.
+void apply_seo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e,
+               bool reduce) {
+  ensure_sym(c, prec);
+  const PrecFields& f = c->pf[pidx(prec)];
+  if (!dag) {
+    hop(c, prec, 0, HOP_CLOV, false, 1.0, in, tmp_e, nullptr, f.clovinv, false);
+    hop(c, prec, 1, HOP_CLOV, false, 0.25, tmp_e, out, nullptr, f.clovinv_odd, false);
+  } else {
+    Spinor to = sub(workspace(c, 900 + pidx(prec), prec, in.nrhs), 0, in.nrhs);
+    blas_clover(c->g, f.clovinv_odd, to, in, c->stream);
+    hop(c, prec, 0, HOP_CLOV, true, 1.0, to, tmp_e, nullptr, f.clovinv, false);
+    hop(c, prec, 1, HOP_PLAIN, true, 0.25, tmp_e, out, nullptr, nullptr, false);
+  }
+  blas_xmy_norm2(c->g, in, out, red(c), c->stream);
+  (void)reduce;
 }
 
 }  // namespace gbc
@@ -418,7 +452,8 @@ int gbc_load_gauge(gbc_ctx* c, const double* links) {
     int* d_nneg = nullptr;
     GBC_CUDA(cudaMalloc(&d_logdet, sizeof(double) * V));
     GBC_CUDA(cudaMalloc(&d_nneg, sizeof(int) * V));
-    clover_build(c->dims, c->d_links, cc, c->d_clov, c->d_inv, d_logdet, d_nneg, 0, c->stream);
+    // A^-1 on both parities: the asymmetric operator needs A_ee^-1, the symmetric one A_oo^-1 too
+    clover_build(c->dims, c->d_links, cc, c->d_clov, c->d_inv, d_logdet, d_nneg, 2, c->stream);
     GBC_CUDA(cudaGetLastError());
     std::vector<double> ld(V);
     std::vector<int> nn(V);
@@ -427,9 +462,17 @@ int gbc_load_gauge(gbc_ctx* c, const double* links) {
     sync(c);
     cudaFree(d_logdet);
     cudaFree(d_nneg);
+    // log det and negative pivots of A_ee (Chroma's cholesDet(0))
     double s = 0;
     int n = 0;
     for (long i = 0; i < V; ++i) {
+      long r = i;
+      int par = 0;
+      for (int k = 0; k < 4; ++k) {
+        par += (int)(r % c->dims[k]);
+        r /= c->dims[k];
+      }
+      if (par & 1) continue;
       s += ld[i];
       n += nn[i];
     }
@@ -447,6 +490,10 @@ int gbc_load_clover(gbc_ctx* c, const double* clov, const double* invclov) {
   return guarded(c, [&]() {
     GBC_CUDA(cudaMemcpyAsync(c->d_clov, clov, sizeof(double) * 72 * c->V, cudaMemcpyHostToDevice, c->stream));
     GBC_CUDA(cudaMemcpyAsync(c->d_inv, invclov, sizeof(double) * 72 * c->V, cudaMemcpyHostToDevice, c->stream));
+    // the caller's inverse is used on the even sites; the odd inverse (symmetric operator) is
+    // built here from the clover term itself
+    clover_invert_parity(c->dims, c->d_clov, c->d_inv, 1, c->stream);
+    GBC_CUDA(cudaGetLastError());
     sync(c);
     return rebuild_from_clover(c);
   });
@@ -470,8 +517,9 @@ int gbc_apply(gbc_ctx* c, int op, int isign, int cb, int prec, int nrhs, double*
   if (isign != 1 && isign != -1) return GBC_ERR_ARGS;
   if (prec != GBC_PREC_DOUBLE && prec != GBC_PREC_SINGLE && prec != GBC_PREC_HALF) return GBC_ERR_ARGS;
   if (!c->have_gauge) return fail(c, GBC_ERR_STATE, "load the gauge field first");
-  if (op < 0 || op > 5 || cb < 0 || cb > 1) return GBC_ERR_ARGS;
-  if (op == GBC_OP_CLOVINV && cb != 0) return GBC_ERR_ARGS;
+  if (op < 0 || op > 7 || cb < 0 || cb > 1) return GBC_ERR_ARGS;
+  if ((op == GBC_OP_SYM || op == GBC_OP_SYM_MDAGM) && c->act.twisted)
+    return fail(c, GBC_ERR_ARGS, "the symmetric operator is not built with a twisted-mass term");
   return guarded(c, [&]() {
     ensure_prec(c, prec);
     ensure_stage(c, nrhs);
@@ -499,8 +547,11 @@ int gbc_apply(gbc_ctx* c, int op, int isign, int cb, int prec, int nrhs, double*
         break;
       case GBC_OP_MEO:
       case GBC_OP_MDAGM:
+      case GBC_OP_SYM:
+      case GBC_OP_SYM_MDAGM: {
         import_spinor(c->g, c->d_stage[0], rs, 1, a, c->stream);
-        if (op == GBC_OP_MEO) {
+        SymScope scope(c, op == GBC_OP_SYM || op == GBC_OP_SYM_MDAGM);
+        if (op == GBC_OP_MEO || op == GBC_OP_SYM) {
           apply_meo(c, prec, dag, a, b, t, false);
         } else {
           apply_meo(c, prec, false, a, d, t, false);
@@ -508,6 +559,7 @@ int gbc_apply(gbc_ctx* c, int op, int isign, int cb, int prec, int nrhs, double*
         }
         export_spinor(c->g, c->d_stage[1], rs, 1, b, c->stream);
         break;
+      }
       case GBC_OP_UNPREC: {
         // chi_e = A_ee psi_e - 1/2 D_eo psi_o ;  chi_o = A_oo psi_o - 1/2 D_oe psi_e
         import_spinor(c->g, c->d_stage[0], rs, 0, a, c->stream);

@@ -21,7 +21,8 @@ struct PrecFields {
   int recon = 18;
   void* gauge[2][4] = {{nullptr}};  // [parity][mu]
   void* clov[2] = {nullptr, nullptr};
-  void* clovinv = nullptr;  // even parity
+  void* clovinv = nullptr;      // A^-1, even parity
+  void* clovinv_odd = nullptr;  // A^-1, odd parity (symmetric operator only; packed on first use)
 };
 
 struct CudaError {
@@ -50,7 +51,7 @@ struct gbc_ctx {
   // canonical FP64 copies on the device
   double* d_links = nullptr;  // [V][4][3][3] complex = 72 doubles per site
   double* d_clov = nullptr;   // [V][72]
-  double* d_inv = nullptr;    // [V][72] (even sites)
+  double* d_inv = nullptr;    // [V][72] A^-1 (both parities)
   double logdet_even = 0;
   int nneg = 0;
 
@@ -94,6 +95,8 @@ struct gbc_ctx {
 
   // learned preconditioner (opaque, owned by precond.cu)
   void* precond = nullptr;
+  // apply_meo applies the symmetric operator M_s instead of M~ (set for a GBC_SYS_SYM* solve)
+  bool sym = false;
 };
 
 namespace gbc {
@@ -113,6 +116,16 @@ void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, con
 // out_o = M~ in_o (dag: M~^dag); reduce => |out|^2 in red(c).result[0][rhs]
 void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, bool reduce);
 void apply_clover(gbc_ctx* c, int prec, int parity, bool inverse, const Spinor& in, const Spinor& out);
+// out_o = M_s in_o (dag: M_s^dag), the symmetric operator; reduce => |out|^2 as apply_meo
+void apply_seo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, bool reduce);
+void ensure_sym(gbc_ctx* c, int prec);  // pack A_oo^-1 in this precision
+// routes apply_meo to the symmetric operator while it lives
+struct SymScope {
+  gbc_ctx* c;
+  bool old;
+  SymScope(gbc_ctx* c_, bool on) : c(c_), old(c_->sym) { c->sym = on; }
+  ~SymScope() { c->sym = old; }
+};
 void sync(gbc_ctx* c);
 double now();
 

@@ -125,11 +125,13 @@ struct CloverCoeffs {
   double coef[6];  // clover coefficient (with the 1/2) of the planes 01,02,03,12,13,23
 };
 // clov[V][72] = packed A (all sites); inv[V][72] = packed A^-1 on the sites of parity inv_parity
-// (zero elsewhere); logdet[V] = sum log|d_i| of the LDL^dag factors on those sites, nneg[V] the
-// number of negative d_i.
+// (2: both parities; zero elsewhere); logdet[V] = sum log|d_i| of the LDL^dag factors on those
+// sites, nneg[V] the number of negative d_i.
 void clover_build(const int dims[4], const double* canon_links, const CloverCoeffs& cc, double* clov, double* inv,
                   double* logdet, int* nneg, int inv_parity, cudaStream_t s);
 void clover_invert(long nsites, double* packed, double* logdet, int* nneg, cudaStream_t s);
+// inv = A^-1 on the sites of one parity, from the packed clov of all sites (canonical order)
+void clover_invert_parity(const int dims[4], const double* clov, double* inv, int parity, cudaStream_t s);
 
 // ---- BLAS-1 and reductions (blas.cu) ----------------------------------------------------------
 // Every vector argument is a Spinor of Vh sites and nrhs right-hand sides; coefficient arrays

@@ -522,8 +522,22 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   if (p.nkrylov <= 0) p.nkrylov = 16;
   int sloppy = p.sloppy_precision ? p.sloppy_precision : c->opts.sloppy_precision;
   if (sloppy != PREC_HALF && sloppy != PREC_SINGLE && sloppy != PREC_DOUBLE) return GBC_ERR_ARGS;
-  if (p.system < GBC_SYS_MEO || p.system > GBC_SYS_FULL) return GBC_ERR_ARGS;
+  if (p.system < GBC_SYS_MEO || p.system > GBC_SYS_SYM_MDAGM) return GBC_ERR_ARGS;
   if (p.solver < GBC_SOLVER_CG || p.solver > GBC_SOLVER_FGMRES) return GBC_ERR_ARGS;
+  // the symmetric operator M_s: every solver below runs unchanged, apply_meo applies M_s
+  const bool symmetric = p.system == GBC_SYS_SYM || p.system == GBC_SYS_SYM_MDAGM;
+  if (symmetric) {
+    if (c->act.twisted) {
+      c->err = "the symmetric operator is not built with a twisted-mass term";
+      return GBC_ERR_ARGS;
+    }
+    if (p.use_precond) {
+      c->err = "the learned preconditioner approximates M~^-1, not the symmetric operator's inverse";
+      return GBC_ERR_ARGS;
+    }
+    p.system = p.system == GBC_SYS_SYM ? GBC_SYS_MEO : GBC_SYS_MDAGM;
+  }
+  SymScope sym_scope(c, symmetric);
 
   const int D = PREC_DOUBLE;
   const Geom& g = c->g;
@@ -533,6 +547,14 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   if (p.solver != GBC_SOLVER_CG) {
     ensure_prec(c, sloppy);
     ensure_prec(c, PREC_SINGLE);
+  }
+  if (symmetric) {
+    // A_oo^-1 packed before any iteration is captured into a graph
+    ensure_sym(c, D);
+    if (p.solver != GBC_SOLVER_CG) {
+      ensure_sym(c, sloppy);
+      ensure_sym(c, PREC_SINGLE);
+    }
   }
   cudaEvent_t ev0, ev1;
   GBC_CUDA(cudaEventCreate(&ev0));

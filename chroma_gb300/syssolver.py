@@ -142,8 +142,17 @@ class SysSolverGB300CloverParams:
 
 class _Base:
     system = G.SYS_MEO
+    symmetric_system = None
 
-    def __init__(self, links, dims, params: SysSolverGB300CloverParams, max_rhs=12):
+    def __init__(self, links, dims, params: SysSolverGB300CloverParams, max_rhs=12, operator="EOPREC_CLOVER"):
+        """operator: the FermAct whose LinearOperator the solver inverts; "SEOPREC_CLOVER" selects the
+        symmetric operator M_s (SymEvenOddPrecCloverLinOp) instead of M~ (EvenOddPrecCloverLinOp)."""
+        if operator == "SEOPREC_CLOVER":
+            if self.symmetric_system is None:
+                raise ValueError(f"{type(self).__name__} has no symmetric form")
+            self.system = self.symmetric_system
+        elif operator != "EOPREC_CLOVER":
+            raise ValueError(f"unsupported operator {operator}")
         self.params = params
         cp = params.CloverParams
         aniso = {"xi_0": cp.xi_0, "nu": cp.nu, "t_dir": cp.t_dir} if cp.anisoP else None
@@ -188,16 +197,20 @@ class _Base:
 
 
 class LinOpSysSolverGB300Clover(_Base):
-    """LinOpSystemSolver<LatticeFermion>: M~ psi_o = chi_o (only rb[1] of psi/chi meaningful)."""
+    """LinOpSystemSolver<LatticeFermion>: M~ psi_o = chi_o (only rb[1] of psi/chi meaningful), or
+    M_s psi_o = chi_o for a SEOPREC_CLOVER action."""
     system = G.SYS_MEO
+    symmetric_system = G.SYS_SYM
 
     def __call__(self, psi, chi):
         return self._solve(psi, chi)
 
 
 class MdagMSysSolverGB300Clover(_Base):
-    """MdagMSystemSolver<LatticeFermion>: M~^dag M~ psi = chi (chronological predictor: psi guess)."""
+    """MdagMSystemSolver<LatticeFermion>: M~^dag M~ psi = chi (chronological predictor: psi guess), or
+    M_s^dag M_s psi = chi for a SEOPREC_CLOVER action."""
     system = G.SYS_MDAGM
+    symmetric_system = G.SYS_SYM_MDAGM
 
     def __call__(self, psi, chi, predictor=None):
         if predictor is not None:
@@ -223,11 +236,11 @@ class _Factory:
         self._creators[name] = creator
         return True
 
-    def createObject(self, name, xml, path, links, dims):
+    def createObject(self, name, xml, path, links, dims, operator="EOPREC_CLOVER"):
         if name not in self._creators:
             # objfactory.h:44-53 throws a string on an unknown key
             raise KeyError(f"Factory error: unknown id {name}")
-        return self._creators[name](xml, path, links, dims)
+        return self._creators[name](xml, path, links, dims, operator)
 
     def keys(self):
         return sorted(self._creators)
@@ -237,9 +250,9 @@ TheLinOpFermSystemSolverFactory = _Factory()
 TheMdagMFermSystemSolverFactory = _Factory()
 TheLinOpFermSystemSolverFactory.registerObject(
     "GB300_CLOVER_INVERTER",
-    lambda xml, path, links, dims: LinOpSysSolverGB300Clover(links, dims,
-                                                             SysSolverGB300CloverParams.from_xml(xml, path)))
+    lambda xml, path, links, dims, operator="EOPREC_CLOVER": LinOpSysSolverGB300Clover(
+        links, dims, SysSolverGB300CloverParams.from_xml(xml, path), operator=operator))
 TheMdagMFermSystemSolverFactory.registerObject(
     "GB300_CLOVER_INVERTER",
-    lambda xml, path, links, dims: MdagMSysSolverGB300Clover(links, dims,
-                                                             SysSolverGB300CloverParams.from_xml(xml, path)))
+    lambda xml, path, links, dims, operator="EOPREC_CLOVER": MdagMSysSolverGB300Clover(
+        links, dims, SysSolverGB300CloverParams.from_xml(xml, path), operator=operator))

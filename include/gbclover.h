@@ -49,10 +49,13 @@ extern "C" {
 /* operators for gbc_apply (parity tests; mirror the EvenOddPrecLinearOperator blocks) */
 #define GBC_OP_DSLASH 0   /* D' on output parity cb (lwldslash_w.h:226-303)                         */
 #define GBC_OP_CLOVER 1   /* A on parity cb (clover_term_qdp_w.h:2138-2160)                         */
-#define GBC_OP_CLOVINV 2  /* A^-1 on the even parity (invclov, eoprec_clover_linop_w.cc:75-86)       */
+#define GBC_OP_CLOVINV 2  /* A^-1 on parity cb (invclov, eoprec_clover_linop_w.cc:75-86; odd: seoprec) */
 #define GBC_OP_MEO 3      /* M~ = A_oo - 1/4 D_oe A_ee^-1 D_eo on odd sites (eoprec_clover_linop_w.cc:142-187) */
 #define GBC_OP_MDAGM 4    /* M~^dag M~ (lib/lmdagm.h)                                                */
 #define GBC_OP_UNPREC 5   /* full unpreconditioned M (lib/eoprec_linop.h:147-165)                    */
+#define GBC_OP_SYM 6      /* M_s = 1 - 1/4 A_oo^-1 D_oe A_ee^-1 D_eo on odd sites
+                             (SymEvenOddPrecCloverLinOp, seoprec_clover_linop_w.cc:145-187)          */
+#define GBC_OP_SYM_MDAGM 7 /* M_s^dag M_s                                                           */
 /* solvers (Chroma invType they stand in for) */
 #define GBC_SOLVER_CG 0           /* CG_INVERTER: CGNE, InvCG2 (invcg2.cc:70-232), FP64           */
 #define GBC_SOLVER_RELIABLE_CG 1  /* RELIABLE_CG_MP_CLOVER_INVERTER (reliable_cg.cc:10-188)         */
@@ -66,6 +69,9 @@ extern "C" {
 #define GBC_SYS_MDAGM 1  /* M~^dag M~ psi_o = chi_o    (MdagMSystemSolver, syssolver_mdagm.h:25-35)    */
 #define GBC_SYS_FULL 2   /* M psi = chi on both parities: Schur prep, odd solve, even reconstruction
                             (PrecFermActQprop, eoprec_fermact_qprop.cc:41-80)                        */
+#define GBC_SYS_SYM 3    /* M_s psi_o = chi_o for the symmetric operator SEOPREC_CLOVER
+                            (SymEvenOddPrecCloverLinOp, seoprec_clover_linop_w.cc:145-187); no twist */
+#define GBC_SYS_SYM_MDAGM 4 /* M_s^dag M_s psi_o = chi_o (MdagM solver of a SEOPREC action)            */
 
 /* ---- parameter structs ------------------------------------------------------------------- */
 typedef struct gbc_geom {

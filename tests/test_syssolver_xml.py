@@ -70,6 +70,12 @@ def test_factories():
     assert not SS.TheLinOpFermSystemSolverFactory.registerObject("GB300_CLOVER_INVERTER", lambda *a: None)
     with pytest.raises(KeyError):
         SS.TheLinOpFermSystemSolverFactory.createObject("NOPE", QUDA_XML, ".", None, None)
+    # an operator the solver does not invert is refused before any device work
+    with pytest.raises(ValueError):
+        SS.TheLinOpFermSystemSolverFactory.createObject("GB300_CLOVER_INVERTER", QUDA_XML, ".", None, None,
+                                                        operator="UNPRECONDITIONED_WILSON")
+    with pytest.raises(ValueError):
+        SS.PrecFermActQprop(None, None, SS.SysSolverGB300CloverParams.from_xml(QUDA_XML), operator="SEOPREC_CLOVER")
 
 
 def test_unknown_solver_type():
