@@ -387,8 +387,13 @@ def main():
     sec1, byts1 = ctx.time_operator(G.OP_DSLASH, G.PREC_HALF, nrhs=1, iters=20, flush_l2=True)
     sec64, byts64 = ctx.time_operator(G.OP_DSLASH, G.PREC_DOUBLE, nrhs=1, iters=10, flush_l2=True)
     achieved = byts / sec / 1e9
+    # DRAM traffic of this launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of the same
+    # kernel on 24^3x48 (456.7 MB for Vh = 331776 sites, 12 RHS), scaled to this lattice by the
+    # number of sites (profiles/hop_kernel_fp16_12rhs_24x24x24x48.md)
+    traffic = 456.7e6 / 331776 * (V // 2)
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+            "frac": achieved / pk["hbm_gbs"], "traffic": traffic, "traffic_source": "ncu, 24^3x48 scaled by sites",
+            "peak_kind": pk_kind,
             "kernel": "hop_kernel<PrecH,12,HOP_PLAIN> 12 RHS (Dslash, FP16 storage, 12-real links)",
             "bytes_per_launch": byts, "seconds_per_launch": sec,
             "single_rhs_fp16_gbs": byts1 / sec1 / 1e9, "single_rhs_fp64_gbs": byts64 / sec64 / 1e9}
