@@ -5,6 +5,7 @@
 
 #include "actions/ferm/invert/syssolver_linop_factory.h"
 #include "actions/ferm/invert/syssolver_mdagm_factory.h"
+#include "actions/ferm/linop/seoprec_clover_linop_w.h"
 
 namespace Chroma
 {
@@ -170,17 +171,23 @@ namespace Chroma
     }
   }  // namespace
 
+  bool is_symmetric_clover(const Handle<LinearOperator<LatticeFermion> >& A)
+  {
+    return dynamic_cast<const SymEvenOddPrecCloverLinOp*>(A.operator->()) != nullptr;
+  }
+
   LinOpSysSolverGB300Clover::LinOpSysSolverGB300Clover(Handle<LinearOperator<T> > A_,
                                                        Handle<FermState<T, Q, Q> > state_,
                                                        const SysSolverGB300CloverParams& p)
-    : A(A_), state(state_), invParam(p), dev(new GB300CloverContext(state_, p))
+    : A(A_), state(state_), invParam(p), dev(new GB300CloverContext(state_, p)),
+      system(is_symmetric_clover(A_) ? GBC_SYS_SYM : GBC_SYS_MEO)
   {}
 
   SystemSolverResults_t LinOpSysSolverGB300Clover::operator()(T& psi, const T& chi) const
   {
     START_CODE();
     bool failed = false;
-    SystemSolverResults_t res = run(*dev, invParam, GBC_SYS_MEO, psi, chi, failed);
+    SystemSolverResults_t res = run(*dev, invParam, system, psi, chi, failed);
     if (failed) {
       // RsdToleranceFactor / SilentFail / BackupSolverParam (syssolver_linop_clover_quda_w.h:636-643)
       if (invParam.backup_invP) {
@@ -204,13 +211,14 @@ namespace Chroma
   MdagMSysSolverGB300Clover::MdagMSysSolverGB300Clover(Handle<LinearOperator<T> > A_,
                                                        Handle<FermState<T, Q, Q> > state_,
                                                        const SysSolverGB300CloverParams& p)
-    : A(A_), state(state_), invParam(p), dev(new GB300CloverContext(state_, p))
+    : A(A_), state(state_), invParam(p), dev(new GB300CloverContext(state_, p)),
+      system(is_symmetric_clover(A_) ? GBC_SYS_SYM_MDAGM : GBC_SYS_MDAGM)
   {}
 
   SystemSolverResults_t MdagMSysSolverGB300Clover::operator()(T& psi, const T& chi) const
   {
     bool failed = false;
-    SystemSolverResults_t res = run(*dev, invParam, GBC_SYS_MDAGM, psi, chi, failed);
+    SystemSolverResults_t res = run(*dev, invParam, system, psi, chi, failed);
     if (failed && !invParam.SilentFail) {
       QDPIO::cerr << "GB300_CLOVER_INVERTER (MdagM): solve failed" << std::endl;
       QDP_abort(1);

@@ -44,7 +44,12 @@ namespace Chroma
     gbc_ctx* ctx;
   };
 
-  //! Solves M~ psi_o = chi_o (only rb[1] meaningful), M~ = A_oo - 1/4 D_oe A_ee^-1 D_eo
+  //! GBC_SYS_SYM* when A is the symmetric operator of a SEOPREC_CLOVER action
+  //! (SymEvenOddPrecCloverLinOp, seoprec_clover_linop_w.h), else the asymmetric systems
+  bool is_symmetric_clover(const Handle<LinearOperator<LatticeFermion> >& A);
+
+  //! Solves M~ psi_o = chi_o (only rb[1] meaningful), M~ = A_oo - 1/4 D_oe A_ee^-1 D_eo, or
+  //! M_s psi_o = chi_o, M_s = 1 - 1/4 A_oo^-1 D_oe A_ee^-1 D_eo, for a symmetric operator A
   class LinOpSysSolverGB300Clover : public LinOpSystemSolver<LatticeFermion>
   {
   public:
@@ -60,9 +65,11 @@ namespace Chroma
     Handle<FermState<T, Q, Q> > state;
     SysSolverGB300CloverParams invParam;
     Handle<GB300CloverContext> dev;
+    int system;
   };
 
-  //! Solves M~^dag M~ psi = chi (HMC), with the chronological predictor as initial guess
+  //! Solves M~^dag M~ psi = chi (HMC; M_s^dag M_s for a symmetric A), with the chronological
+  //! predictor as initial guess
   class MdagMSysSolverGB300Clover : public MdagMSystemSolver<LatticeFermion>
   {
   public:
@@ -79,6 +86,7 @@ namespace Chroma
     Handle<FermState<T, Q, Q> > state;
     SysSolverGB300CloverParams invParam;
     Handle<GB300CloverContext> dev;
+    int system;
   };
 
 }  // namespace Chroma
