@@ -3,6 +3,7 @@
 // the autotuner chooses from (TX sites x NRB right-hand sides per block, MINB resident blocks).
 #pragma once
 #include "dslash.cuh"
+#include "dslash_async.cuh"
 
 namespace gbc {
 
@@ -25,19 +26,30 @@ static int hop_shape(const HopArgs& a, HopShape sh, cudaStream_t s) {
   GBC_SHAPE(32, 12, 2)
 #undef GBC_SHAPE
   if constexpr (std::is_same<P, PrecH>::value) {
-    // two sites per thread: blocks of TX threads cover 2 TX sites
-    if (!sh.pair || sh.nrb != 1 || (a.g.L[3] & 1)) return -1;
-    auto go2 = [&](auto kern, int tx) {
-      const int nbp = (a.g.Vh / 2 + tx - 1) / tx;
-      kern<<<(unsigned)(nbp * a.nrhs), tx, 0, s>>>(a);
-      return nbp;
-    };
+    if (sh.nrb != 1) return -1;
+    if (sh.pair == 1) {
+      // two sites per thread: blocks of TX threads cover 2 TX sites
+      if (a.g.L[3] & 1) return -1;
+      auto go2 = [&](auto kern, int tx) {
+        const int nbp = (a.g.Vh / 2 + tx - 1) / tx;
+        kern<<<(unsigned)(nbp * a.nrhs), tx, 0, s>>>(a);
+        return nbp;
+      };
 #define GBC_PAIR(TX, MINB) \
   if (sh.tx == TX && sh.minb == MINB) return go2(hop_kernel_pair<RECON, MODE, DAG, REDUCE, TX, MINB>, TX);
-    GBC_PAIR(128, 2)
-    GBC_PAIR(128, 3)
-    GBC_PAIR(64, 6)
+      GBC_PAIR(128, 2)
+      GBC_PAIR(128, 3)
+      GBC_PAIR(64, 6)
 #undef GBC_PAIR
+    } else if (sh.pair == 2) {
+      // the next hops' loads in flight through a shared-memory ring (one site per thread)
+#define GBC_ASYNC(TX, MINB) \
+  if (sh.tx == TX && sh.minb == MINB) return go(hop_kernel_async<RECON, MODE, DAG, REDUCE, TX, MINB>, TX, 1);
+      GBC_ASYNC(128, 3)
+      GBC_ASYNC(128, 4)
+      GBC_ASYNC(64, 8)
+#undef GBC_ASYNC
+    }
   }
   return -1;
 }

@@ -57,7 +57,8 @@ struct HopArgs {
 
 // Launch geometry chosen by the caller (autotuned): TX sites x NRB right-hand sides per block,
 // MINB resident blocks per SM requested from the register allocator.  pair = 1: the fp16 kernel
-// with two sites per thread (TX threads cover 2 TX sites; fp16 storage and even Lt only).
+// with two sites per thread (TX threads cover 2 TX sites; fp16 storage and even Lt only);
+// pair = 2: the fp16 kernel that streams the next hops through a shared-memory ring (cp.async).
 struct HopShape {
   int tx;
   int nrb;
@@ -65,13 +66,15 @@ struct HopShape {
   int pair;
 };
 // the compiled candidates (dslash_inst.cuh)
-constexpr HopShape kHopShapes[] = {{128, 1, 1, 0}, {128, 1, 6, 0}, {32, 4, 1, 0},  {32, 4, 5, 0},  {64, 2, 4, 0},
-                                   {32, 12, 2, 0}, {128, 1, 2, 1}, {128, 1, 3, 1}, {64, 1, 6, 1}};
-constexpr int kNumHopShapes = 9;
+constexpr HopShape kHopShapes[] = {{128, 1, 1, 0}, {128, 1, 6, 0}, {32, 4, 1, 0},  {32, 4, 5, 0},
+                                   {64, 2, 4, 0},  {32, 12, 2, 0}, {128, 1, 2, 1}, {128, 1, 3, 1},
+                                   {64, 1, 6, 1},  {128, 1, 3, 2}, {128, 1, 4, 2}, {64, 1, 8, 2}};
+constexpr int kNumHopShapes = 12;
 // whether shape sh can run the hopping term of precision prec over nrhs right-hand sides of a
 // lattice with time extent lt
 inline bool hop_shape_valid(const HopShape& sh, int prec, int nrhs, int lt) {
-  if (sh.pair) return prec == PREC_HALF && lt % 2 == 0;
+  if (sh.pair == 1) return prec == PREC_HALF && lt % 2 == 0;
+  if (sh.pair == 2) return prec == PREC_HALF;
   return !(sh.nrb > 1 && sh.nrb > nrhs);  // a block would be mostly idle
 }
 

@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 KAPPA = 0.115
 CSW = 1.0
-NUM_SHAPES = 9  # the candidates compiled into the library (kHopShapes)
+NUM_SHAPES = 12  # the candidates compiled into the library (kHopShapes)
 
 
 def rel(a, b):
