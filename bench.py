@@ -385,6 +385,9 @@ def main():
     pk, pk_kind = peaks()
     sec, byts = ctx.time_operator(G.OP_DSLASH, G.PREC_HALF, nrhs=12, iters=20, flush_l2=True)
     sec1, byts1 = ctx.time_operator(G.OP_DSLASH, G.PREC_HALF, nrhs=1, iters=20, flush_l2=True)
+    # the whole even-odd operator M~ (two fused launches, clover epilogues), one RHS, FP16:
+    # algorithmic bytes Vh (16L + 2C + 5S)
+    secm, bytm = ctx.time_operator(G.OP_MEO, G.PREC_HALF, nrhs=1, iters=20, flush_l2=True)
     sec64, byts64 = ctx.time_operator(G.OP_DSLASH, G.PREC_DOUBLE, nrhs=1, iters=10, flush_l2=True)
     achieved = byts / sec / 1e9
     # DRAM traffic of this launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of the same
@@ -396,7 +399,9 @@ def main():
             "peak_kind": pk_kind,
             "kernel": "hop_kernel<PrecH,12,HOP_PLAIN> 12 RHS (Dslash, FP16 storage, 12-real links)",
             "bytes_per_launch": byts, "seconds_per_launch": sec,
-            "single_rhs_fp16_gbs": byts1 / sec1 / 1e9, "single_rhs_fp64_gbs": byts64 / sec64 / 1e9}
+            "single_rhs_fp16_gbs": byts1 / sec1 / 1e9, "single_rhs_fp16_frac": byts1 / sec1 / 1e9 / pk["hbm_gbs"],
+            "single_rhs_meo_fp16_gbs": bytm / secm / 1e9, "single_rhs_meo_fp16_frac": bytm / secm / 1e9 / pk["hbm_gbs"],
+            "single_rhs_fp64_gbs": byts64 / sec64 / 1e9}
 
     # e2e through the public API with pinned host buffers
     chi_h = torch.from_numpy(src.view(np.float64).copy()).pin_memory()

@@ -594,6 +594,10 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   const bool mdagm = p.system == GBC_SYS_MDAGM;
   std::vector<int> iters(n, 0), status(n, GBC_OK), outer(n, 0);
   int reliable = 0;
+  // |chi - A psi|^2 in FP64 for the final psi, when the solver has just computed it (the last
+  // outer residual of the defect correction, the last restart check of CG): the final check
+  // then reuses it instead of applying the FP64 operator again
+  std::vector<double> known_rr;
 
   if (p.solver == GBC_SOLVER_CG) {
     // chi' = M~^dag chi (LinOp) ; InvCG2 on M~^dag M~
@@ -622,6 +626,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
       apply_sys(c, D, mdagm, psi, t1, t2, ted);
       blas_xmy_norm2(g, chi, t1, red(c), s);
       std::vector<double> rr = fetch(c, 1, n);
+      known_rr = rr;
       double worst_rel = 0;
       bool any = false;
       for (int i = 0; i < n; ++i) {
@@ -711,7 +716,10 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
           worst = std::max(worst, std::sqrt(rr[i] / bb[i]));
         }
       }
-      if (all || it == max_outer || total >= p.max_iter) break;
+      if (all || it == max_outer || total >= p.max_iter) {
+        known_rr = rr;
+        break;
+      }
       std::vector<int> active(n);
       for (int i = 0; i < n; ++i) {
         active[i] = !done[i];
@@ -752,10 +760,18 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   }
 
   // true FP64 residual of the system solved, then even reconstruction for the full system
+  // (the full system reports the residual of M over both parities, computed below instead)
   std::vector<double> bb = norm2(c, chi);
-  apply_sys(c, D, mdagm, psi, t1, t2, ted);
-  blas_xmy_norm2(g, chi, t1, red(c), s);
-  std::vector<double> rr = fetch(c, 1, n);
+  std::vector<double> rr(n, 0.0);
+  if (p.system != GBC_SYS_FULL) {
+    if (known_rr.size() == (size_t)n) {
+      rr = known_rr;
+    } else {
+      apply_sys(c, D, mdagm, psi, t1, t2, ted);
+      blas_xmy_norm2(g, chi, t1, red(c), s);
+      rr = fetch(c, 1, n);
+    }
+  }
   export_spinor(g, psi_canon, rs, 1, psi, s);
   if (p.system == GBC_SYS_FULL) {
     // psi_e = A_ee^-1 (chi_e + 1/2 D_eo psi_o)   (eoprec_fermact_qprop.cc:60-67)
@@ -763,14 +779,15 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     blas_xpy(g, t1, chie, s);
     apply_clover(c, D, 0, true, t1, psie);
     export_spinor(g, psi_canon, rs, 0, psie, s);
-    // full residual |M psi - chi| over both parities (eoprec_fermact_qprop.cc:70-76)
-    Spinor ue = sub(workspace(c, SLOT_T1, D, n), 0, n);
+    // full residual |M psi - chi| over both parities (eoprec_fermact_qprop.cc:70-76); the even
+    // part A_ee psi_e - 1/2 D_eo psi_o - chi_e reuses t1 = chi_e + 1/2 D_eo psi_o from above
+    Spinor ue = sub(workspace(c, SLOT_T2 + 50, D, n), 0, n);
     Spinor uo = sub(workspace(c, SLOT_T2, D, n), 0, n);
-    hop(c, D, 0, HOP_XPAY, false, -0.5, psi, ue, &psie, fd.clov[0], false);
+    apply_clover(c, D, 0, false, psie, ue);
     hop(c, D, 1, HOP_XPAY, false, -0.5, psie, uo, &psi, fd.clov[1], false);
     Spinor chio = sub(workspace(c, SLOT_PSIE + 50, D, n), 0, n);
     import_spinor(g, chi_canon, rs, 1, chio, s);
-    blas_xmy_norm2(g, chie, ue, red(c), s);
+    blas_xmy_norm2(g, t1, ue, red(c), s);
     std::vector<double> re = fetch(c, 1, n);
     blas_xmy_norm2(g, chio, uo, red(c), s);
     std::vector<double> ro = fetch(c, 1, n);
