@@ -36,9 +36,15 @@ namespace {
 constexpr int CT = 128;     // threads per block
 constexpr int SITES = 32;   // sites per block -> 96 rows (site, colour)
 constexpr int ROWS = SITES * 3;
+constexpr int DP = ROWS + 8;  // pitch of the transposed delta tile: 52 words = 4 mod 8 (conflict-free)
 
 __host__ __device__ constexpr int kpad(int cin) { return ((9 * cin * 2 + 15) / 16) * 16; }
 __host__ __device__ constexpr int npad(int cout) { return ((2 * cout + 7) / 8) * 8; }
+
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
 
 __device__ __forceinline__ Coord eo_coords(const Geom& g, int j) {
   const int par = j >= g.Vh ? 1 : 0;
@@ -49,75 +55,82 @@ __device__ __forceinline__ int eo_index(const Geom& g, const Coord& c) {
   return par * g.Vh + cb_index(g, c);
 }
 
-// neighbour site and link (row-major 3x3, already daggered for backward hops) of direction d
-__device__ __forceinline__ int hop_site(const Geom& g, const float2* links, int j, int d, float2 (&u)[9]) {
-  Coord c = eo_coords(g, j);
-  const int mu = (d - 1) >> 1;
-  const bool bwd = ((d - 1) & 1) != 0;
-  if (!bwd) {
-    const float2* L = links + ((size_t)j * 4 + mu) * 9;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) u[k] = L[k];
-    c.x[mu] = c.x[mu] + 1 == g.L[mu] ? 0 : c.x[mu] + 1;
-    return eo_index(g, c);
-  }
-  c.x[mu] = c.x[mu] == 0 ? g.L[mu] - 1 : c.x[mu] - 1;
-  const int n = eo_index(g, c);
-  const float2* L = links + ((size_t)n * 4 + mu) * 9;
-#pragma unroll
-  for (int r = 0; r < 3; ++r)
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float2 e = L[3 * k + r];
-      u[3 * r + k] = make_float2(e.x, -e.y);
-    }
-  return n;
+// Row pitch (bf16 elements) of the staged tiles: at least kpad(cin), with the pitch in 32-bit words
+// = 4 mod 8, so that the 8 rows x 4 column pairs an mma fragment load touches fall in 32 distinct
+// shared-memory banks (a pitch of 224 elements put them on 8 banks: 4-way conflicts).
+__host__ __device__ constexpr int gpitch(int cin) {
+  return kpad(cin) + ((4 - (kpad(cin) / 2) % 8 + 8) % 8) * 2;
 }
 
-// G[row = s*3 + a][k = (d*CIN + i)*2 + re/im] = (T_d h)(site)[i][a] in BF16; pad columns zeroed
-template <int CIN>
-__device__ void gather_tile(__nv_bfloat16* G, const Geom& g, int V, const float2* links, const float2* h, int site0) {
-  constexpr int KP = kpad(CIN);
+// the 9 sites each site of the tile reads (d = 0 itself, 1 + 2 mu forward, 2 + 2 mu backward)
+__device__ void tile_neighbours(int (*nbr)[9], const Geom& g, int V, int site0) {
   for (int p = threadIdx.x; p < SITES * 9; p += blockDim.x) {
-    const int s = p % SITES, d = p / SITES;
+    const int s = p / 9, d = p % 9, j = site0 + s;
+    int n = j;
+    if (j < V && d > 0) {
+      Coord c = eo_coords(g, j);
+      const int mu = (d - 1) >> 1;
+      if (((d - 1) & 1) == 0) c.x[mu] = c.x[mu] + 1 == g.L[mu] ? 0 : c.x[mu] + 1;
+      else c.x[mu] = c.x[mu] == 0 ? g.L[mu] - 1 : c.x[mu] - 1;
+      n = eo_index(g, c);
+    }
+    nbr[s][d] = n;
+  }
+}
+
+// G[row = s*3 + a][k = (d*CIN + i)*2 + re/im] = (T_d h)(site)[i][a] in BF16, row pitch GP; the K
+// padding zeroed.  One task per (site, direction, channel), channel fastest: consecutive threads
+// read consecutive channel vectors and write consecutive 32-bit words (re, im packed), and the
+// link of a (site, direction) is shared through L1 by the threads of its channels.
+template <int CIN>
+__device__ void gather_tile(__nv_bfloat16* G, const int (*nbr)[9], int V, const float2* links, const float2* h,
+                            int site0) {
+  constexpr int GP = gpitch(CIN);
+  for (int p = threadIdx.x; p < SITES * 9 * CIN; p += blockDim.x) {
+    const int i = p % CIN, sd = p / CIN, s = sd % SITES, d = sd / SITES;
     const int j = site0 + s;
-    __nv_bfloat16* row0 = G + (size_t)(s * 3) * KP + d * CIN * 2;
+    uint32_t* row = reinterpret_cast<uint32_t*>(G + (size_t)(s * 3) * GP + (d * CIN + i) * 2);
+    constexpr int RW = GP / 2;  // pitch in 32-bit words
     if (j >= V) {
-      for (int a = 0; a < 3; ++a)
-        for (int k = 0; k < CIN * 2; ++k) row0[a * KP + k] = __float2bfloat16(0.f);
+      row[0] = row[RW] = row[2 * RW] = 0u;
       continue;
     }
+    const int n = nbr[s][d];
+    const float2* src = h + ((size_t)n * CIN + i) * 3;
+    const float2 x0 = src[0], x1 = src[1], x2 = src[2];
     if (d == 0) {
-      const float2* src = h + (size_t)j * CIN * 3;
-      for (int i = 0; i < CIN; ++i)
-        for (int a = 0; a < 3; ++a) {
-          const float2 v = src[i * 3 + a];
-          row0[a * KP + 2 * i] = __float2bfloat16(v.x);
-          row0[a * KP + 2 * i + 1] = __float2bfloat16(v.y);
-        }
+      row[0] = bf16x2(x0.x, x0.y);
+      row[RW] = bf16x2(x1.x, x1.y);
+      row[2 * RW] = bf16x2(x2.x, x2.y);
       continue;
     }
-    float2 u[9];
-    const int n = hop_site(g, links, j, d, u);
-    const float2* src = h + (size_t)n * CIN * 3;
-    for (int i = 0; i < CIN; ++i) {
-      const float2 x0 = src[i * 3], x1 = src[i * 3 + 1], x2 = src[i * 3 + 2];
+    const int mu = (d - 1) >> 1;
+    const bool bwd = ((d - 1) & 1) != 0;
+    // T_{+mu} h = U_mu(x) h(x+mu);  T_{-mu} h = U_mu(x-mu)^dag h(x-mu)
+    const float2* L = links + ((size_t)(bwd ? n : j) * 4 + mu) * 9;
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float2 u0 = u[3 * a], u1 = u[3 * a + 1], u2 = u[3 * a + 2];
-        const float re = u0.x * x0.x - u0.y * x0.y + u1.x * x1.x - u1.y * x1.y + u2.x * x2.x - u2.y * x2.y;
-        const float im = u0.x * x0.y + u0.y * x0.x + u1.x * x1.y + u1.y * x1.x + u2.x * x2.y + u2.y * x2.x;
-        row0[a * KP + 2 * i] = __float2bfloat16(re);
-        row0[a * KP + 2 * i + 1] = __float2bfloat16(im);
+    for (int a = 0; a < 3; ++a) {
+      float2 u0, u1, u2;
+      if (!bwd) {
+        u0 = L[3 * a];
+        u1 = L[3 * a + 1];
+        u2 = L[3 * a + 2];
+      } else {
+        u0 = make_float2(L[a].x, -L[a].y);
+        u1 = make_float2(L[3 + a].x, -L[3 + a].y);
+        u2 = make_float2(L[6 + a].x, -L[6 + a].y);
       }
+      const float re = u0.x * x0.x - u0.y * x0.y + u1.x * x1.x - u1.y * x1.y + u2.x * x2.x - u2.y * x2.y;
+      const float im = u0.x * x0.y + u0.y * x0.x + u1.x * x1.y + u1.y * x1.x + u2.x * x2.y + u2.y * x2.x;
+      row[a * RW] = bf16x2(re, im);
     }
   }
   // zero the K padding
-  constexpr int K = 9 * CIN * 2;
+  constexpr int K = 9 * CIN * 2, KP = kpad(CIN);
   if (KP > K)
     for (int p = threadIdx.x; p < ROWS * (KP - K); p += blockDim.x) {
       const int r = p / (KP - K), k = K + p % (KP - K);
-      G[(size_t)r * KP + k] = __float2bfloat16(0.f);
+      G[(size_t)r * GP + k] = __float2bfloat16(0.f);
     }
 }
 
@@ -138,15 +151,18 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], 
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, const float2* links, const float2* hin,
                                                    float2* hout, const __nv_bfloat16* Wr) {
-  constexpr int KP = kpad(CIN), NP = npad(COUT);
+  constexpr int KP = kpad(CIN), NP = npad(COUT), GP = gpitch(CIN);
   extern __shared__ __align__(16) unsigned char smem[];
   __nv_bfloat16* G = reinterpret_cast<__nv_bfloat16*>(smem);
-  __nv_bfloat16* W = G + ROWS * KP;
+  __nv_bfloat16* W = G + ROWS * GP;  // same pitch: the B fragment loads are conflict-free too
+  __shared__ int nbr[SITES][9];
   const int b = blockIdx.y;
   const int site0 = blockIdx.x * SITES;
   const float2* h = hin + (size_t)b * V * CIN * 3;
-  for (int p = threadIdx.x; p < NP * KP; p += blockDim.x) W[p] = Wr[p];
-  gather_tile<CIN>(G, g, V, links, h, site0);
+  for (int p = threadIdx.x; p < NP * KP; p += blockDim.x) W[(p / KP) * GP + p % KP] = Wr[p];
+  tile_neighbours(nbr, g, V, site0);
+  __syncthreads();
+  gather_tile<CIN>(G, nbr, V, links, h, site0);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gid = lane >> 2, tig = lane & 3;
@@ -156,10 +172,10 @@ __global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, const float2* 
     const int mt = t % MT, nt = t / MT;
     float c[4] = {0.f, 0.f, 0.f, 0.f};
     for (int ks = 0; ks < KP / 16; ++ks) {
-      const __nv_bfloat16* A0 = G + (size_t)(mt * 16 + gid) * KP + ks * 16 + 2 * tig;
-      const __nv_bfloat16* A1 = A0 + 8 * KP;
+      const __nv_bfloat16* A0 = G + (size_t)(mt * 16 + gid) * GP + ks * 16 + 2 * tig;
+      const __nv_bfloat16* A1 = A0 + 8 * GP;
       uint32_t a[4] = {ld_bf16x2(A0), ld_bf16x2(A1), ld_bf16x2(A0 + 8), ld_bf16x2(A1 + 8)};
-      const __nv_bfloat16* B0 = W + (size_t)(nt * 8 + gid) * KP + ks * 16 + 2 * tig;
+      const __nv_bfloat16* B0 = W + (size_t)(nt * 8 + gid) * GP + ks * 16 + 2 * tig;
       uint32_t bb[2] = {ld_bf16x2(B0), ld_bf16x2(B0 + 8)};
       mma_bf16(c, a, bb);
     }
@@ -180,13 +196,16 @@ __global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, const float2* 
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(CT) wgrad_kernel(Geom g, int V, const float2* links, const float2* hin,
                                                    const float2* delta, float* dW) {
-  constexpr int KP = kpad(CIN), NP = npad(COUT), MP = ((NP + 15) / 16) * 16;
+  constexpr int KP = kpad(CIN), NP = npad(COUT), MP = ((NP + 15) / 16) * 16, GP = gpitch(CIN);
   extern __shared__ __align__(16) unsigned char smem[];
   __nv_bfloat16* G = reinterpret_cast<__nv_bfloat16*>(smem);
-  __nv_bfloat16* Dt = G + ROWS * KP;  // [MP][ROWS]: delta transposed (A operand, row-major M x K)
+  __nv_bfloat16* Dt = G + ROWS * GP;  // [MP][DP]: delta transposed (A operand, row-major M x K)
+  __shared__ int nbr[SITES][9];
   const int b = blockIdx.y;
   const int site0 = blockIdx.x * SITES;
-  gather_tile<CIN>(G, g, V, links, hin + (size_t)b * V * CIN * 3, site0);
+  tile_neighbours(nbr, g, V, site0);
+  __syncthreads();
+  gather_tile<CIN>(G, nbr, V, links, hin + (size_t)b * V * CIN * 3, site0);
   const float2* dl = delta + (size_t)b * V * COUT * 3;
   for (int p = threadIdx.x; p < MP * ROWS; p += blockDim.x) {
     const int n = p / ROWS, row = p % ROWS;
@@ -196,7 +215,7 @@ __global__ void __launch_bounds__(CT) wgrad_kernel(Geom g, int V, const float2* 
       const float2 d = dl[((size_t)j * COUT + o) * 3 + a];
       v = (n & 1) ? d.y : d.x;
     }
-    Dt[(size_t)n * ROWS + row] = __float2bfloat16(v);
+    Dt[(size_t)n * DP + row] = __float2bfloat16(v);
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -207,14 +226,14 @@ __global__ void __launch_bounds__(CT) wgrad_kernel(Geom g, int V, const float2* 
     float c[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int ks = 0; ks < ROWS / 16; ++ks) {
-      const __nv_bfloat16* A0 = Dt + (size_t)(mt * 16 + gid) * ROWS + ks * 16 + 2 * tig;
-      const __nv_bfloat16* A1 = A0 + 8 * ROWS;
+      const __nv_bfloat16* A0 = Dt + (size_t)(mt * 16 + gid) * DP + ks * 16 + 2 * tig;
+      const __nv_bfloat16* A1 = A0 + 8 * DP;
       uint32_t a[4] = {ld_bf16x2(A0), ld_bf16x2(A1), ld_bf16x2(A0 + 8), ld_bf16x2(A1 + 8)};
       // B (K = rows x N = k columns), col-major fragment: (k = 2 tig + {0,1}, n = gid)
       const int col = nt * 8 + gid;
       const int r0 = ks * 16 + 2 * tig;
-      uint32_t bb[2] = {pack_bf16(G[(size_t)r0 * KP + col], G[(size_t)(r0 + 1) * KP + col]),
-                        pack_bf16(G[(size_t)(r0 + 8) * KP + col], G[(size_t)(r0 + 9) * KP + col])};
+      uint32_t bb[2] = {pack_bf16(G[(size_t)r0 * GP + col], G[(size_t)(r0 + 1) * GP + col]),
+                        pack_bf16(G[(size_t)(r0 + 8) * GP + col], G[(size_t)(r0 + 9) * GP + col])};
       mma_bf16(c, a, bb);
     }
 #pragma unroll
@@ -328,7 +347,7 @@ __global__ void links_kernel(Geom g, int V, const double2* canon, float2* links)
 template <int CIN, int COUT>
 void launch_layer(const Geom& g, int V, int batch, const float2* links, const float2* in, float2* out,
                   const __nv_bfloat16* W, cudaStream_t s) {
-  const size_t smem = (size_t)(ROWS * kpad(CIN) + npad(COUT) * kpad(CIN)) * 2;
+  const size_t smem = (size_t)(ROWS * gpitch(CIN) + npad(COUT) * gpitch(CIN)) * 2;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(layer_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -343,7 +362,7 @@ template <int CIN, int COUT>
 void launch_wgrad(const Geom& g, int V, int batch, const float2* links, const float2* in, const float2* delta,
                   float* dW, cudaStream_t s) {
   constexpr int MP = ((npad(COUT) + 15) / 16) * 16;
-  const size_t smem = (size_t)(ROWS * kpad(CIN) + MP * ROWS) * 2;
+  const size_t smem = (size_t)(ROWS * gpitch(CIN) + MP * DP) * 2;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(wgrad_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
