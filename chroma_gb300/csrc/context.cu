@@ -167,7 +167,9 @@ static int default_shape(int nrhs) {
 }
 
 int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce, const HopArgs& h) {
-  const long key = ((((long)pidx(prec) * 4 + mode) * 2 + (dag ? 1 : 0)) * 2 + (reduce ? 1 : 0)) * 64 + h.nrhs;
+  // (precision, epilogue, isign, reduction) in the high bits, nrhs (any size) in the low 32
+  const long long key =
+      ((((long long)pidx(prec) * 4 + mode) * 2 + (dag ? 1 : 0)) * 2 + (reduce ? 1 : 0)) << 32 | (unsigned)h.nrhs;
   auto it = c->tuned.find(key);
   if (it != c->tuned.end()) return it->second;
   int best = default_shape(h.nrhs);

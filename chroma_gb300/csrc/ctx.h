@@ -88,7 +88,7 @@ struct gbc_ctx {
   std::map<int, gbc::Spinor> ws;
 
   // autotuned hopping-kernel shapes, keyed by (precision, mode, dagger, reduce, nrhs)
-  std::map<long, int> tuned;
+  std::map<long long, int> tuned;  // autotuner decisions (context.cu tuned_shape)
   bool autotune = true;
   bool use_graphs = true;  // CUDA-graph replay of CG iteration blocks (GBC_GRAPHS=0: off)
   std::string tune_log;
