@@ -153,6 +153,7 @@ void free_ctx_memory(gbc_ctx* c) {
   if (c->h_result) cudaFreeHost(c->h_result);
   if (c->h_cg) cudaFreeHost(c->h_cg);
   if (c->h_coef) cudaFreeHost(c->h_coef);
+  if (c->d_bisc) cudaFree(c->d_bisc);
 }
 
 // Autotuner: the first launch of each (precision, mode, sign, reduction, nrhs) times every compiled

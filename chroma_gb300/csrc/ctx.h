@@ -97,6 +97,9 @@ struct gbc_ctx {
   void* precond = nullptr;
   // apply_meo applies the symmetric operator M_s instead of M~ (set for a GBC_SYS_SYM* solve)
   bool sym = false;
+  // device scalars of the inner BiCGStab (bicgstab.cu), bisc_cap right-hand sides
+  void* d_bisc = nullptr;
+  int bisc_cap = 0;
 };
 
 namespace gbc {
@@ -133,6 +136,17 @@ double now();
 void precond_free(gbc_ctx* c);
 // out ~= M~^-1 in (odd checkerboard fields, same precision, nrhs right-hand sides)
 void precond_apply(gbc_ctx* c, const Spinor& in, const Spinor& out);
+
+// ---- inner BiCGStab (bicgstab.cu) ----------------------------------------------------------------
+struct InnerStats {
+  std::vector<int> iters;
+  std::vector<int> status;
+  int reliable = 0;
+};
+// M~ x = b in the sloppy operator po with accumulator precision pa, relative target tol on the
+// iterated residual, reliable updates at delta; active[r] == 0 leaves right-hand side r at x = 0
+InnerStats bicgstab(gbc_ctx* c, int pa, int po, double tol, int maxit, double delta, const Spinor& x,
+                    const Spinor& b, const std::vector<int>& active);
 
 // ---- solvers (solvers.cu) -------------------------------------------------------------------
 int solve_device(gbc_ctx* c, const gbc_solve_params* p, int nrhs, double* psi_canon, const double* chi_canon,

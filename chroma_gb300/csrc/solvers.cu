@@ -523,7 +523,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   int sloppy = p.sloppy_precision ? p.sloppy_precision : c->opts.sloppy_precision;
   if (sloppy != PREC_HALF && sloppy != PREC_SINGLE && sloppy != PREC_DOUBLE) return GBC_ERR_ARGS;
   if (p.system < GBC_SYS_MEO || p.system > GBC_SYS_SYM_MDAGM) return GBC_ERR_ARGS;
-  if (p.solver < GBC_SOLVER_CG || p.solver > GBC_SOLVER_FGMRES) return GBC_ERR_ARGS;
+  if (p.solver < GBC_SOLVER_CG || p.solver > GBC_SOLVER_BICGSTAB) return GBC_ERR_ARGS;
   // the symmetric operator M_s: every solver below runs unchanged, apply_meo applies M_s
   const bool symmetric = p.system == GBC_SYS_SYM || p.system == GBC_SYS_SYM_MDAGM;
   if (symmetric) {
@@ -651,7 +651,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     iters = st.iters;
     status = st.status;
     reliable = st.reliable;
-  } else if (p.solver == GBC_SOLVER_MIXED || p.solver == GBC_SOLVER_FGMRES) {
+  } else if (p.solver == GBC_SOLVER_MIXED || p.solver == GBC_SOLVER_FGMRES || p.solver == GBC_SOLVER_BICGSTAB) {
     // FP64 defect correction: r = chi - A psi; solve A e = r in low precision; psi += e
     const int S = PREC_SINGLE;
     const int pa = sloppy == PREC_DOUBLE ? D : S;
@@ -756,6 +756,12 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
         // flexible GMRES on M~ e = r directly (preconditioned by the learned network if loaded)
         blas_zero(g, es, s);
         st = fgmres(c, pa, sloppy, es, rsl, itol, p.inner_max_iter, p.nkrylov, p.use_precond != 0, active);
+      } else if (p.solver == GBC_SOLVER_BICGSTAB && !mdagm) {
+        // BiCGStab on M~ e = r directly (no normal equations)
+        InnerStats bs = bicgstab(c, pa, sloppy, itol, p.inner_max_iter, p.delta, es, rsl, active);
+        st.iters = bs.iters;
+        st.status = bs.status;
+        st.reliable = bs.reliable;
       } else {
         if (!mdagm) apply_meo(c, pa, true, rsl, rhs, teh, false);
         else blas_copy(g, rhs, rsl, s);

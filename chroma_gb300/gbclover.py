@@ -20,7 +20,7 @@ ERRORS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "solver did not co
 PREC_HALF, PREC_SINGLE, PREC_DOUBLE = 2, 4, 8
 RECON_18, RECON_12 = 18, 12
 OP_DSLASH, OP_CLOVER, OP_CLOVINV, OP_MEO, OP_MDAGM, OP_UNPREC, OP_SYM, OP_SYM_MDAGM = range(8)
-SOLVER_CG, SOLVER_RELIABLE_CG, SOLVER_MIXED, SOLVER_FGMRES = range(4)
+SOLVER_CG, SOLVER_RELIABLE_CG, SOLVER_MIXED, SOLVER_FGMRES, SOLVER_BICGSTAB = range(5)
 SYS_MEO, SYS_MDAGM, SYS_FULL, SYS_SYM, SYS_SYM_MDAGM = range(5)
 
 # every entry point include/gbclover.h declares

@@ -4,7 +4,8 @@ Mirrors, for Python callers and for the tests, the interface that the C++ adapte
 ``chroma_plugin/`` gives Chroma:
 
 - ``SysSolverGB300CloverParams``: the QUDA clover XML schema (syssolver_quda_clover_params.cc:12-131)
-  plus optional tags (SolverType MIXED/FGMRES, NKrylov, PrecondWeights, InnerTol);
+  plus optional tags (SolverType MIXED/FGMRES/BICGSTAB, NKrylov, PrecondWeights, InnerTol);
+  QUDA's GCR maps to FGMRES (both minimise the residual over a flexible Krylov space);
 - ``TheLinOpFermSystemSolverFactory`` / ``TheMdagMFermSystemSolverFactory``: string-keyed
   factories (syssolver_linop_factory.h:29-39, syssolver_mdagm_factory.h:28-39) with the entry
   ``GB300_CLOVER_INVERTER``;
@@ -26,7 +27,7 @@ from . import gbclover as G
 _PREC = {"HALF": G.PREC_HALF, "SINGLE": G.PREC_SINGLE, "DOUBLE": G.PREC_DOUBLE}
 _RECON = {"RECONS_12": G.RECON_12, "RECONS_NONE": G.RECON_18, "RECONS_18": G.RECON_18, "RECONS_8": G.RECON_12}
 _SOLVER = {"CG": G.SOLVER_CG, "RELIABLE_CG": G.SOLVER_RELIABLE_CG, "MIXED": G.SOLVER_MIXED,
-           "BICGSTAB": G.SOLVER_MIXED, "GCR": G.SOLVER_MIXED, "FGMRES": G.SOLVER_FGMRES}
+           "BICGSTAB": G.SOLVER_BICGSTAB, "GCR": G.SOLVER_FGMRES, "FGMRES": G.SOLVER_FGMRES}
 
 
 class SolverFailure(RuntimeError):

@@ -21,7 +21,8 @@ namespace Chroma
     {
       if (s == "CG") return GBC_SOLVER_CG;
       if (s == "RELIABLE_CG") return GBC_SOLVER_RELIABLE_CG;
-      if (s == "FGMRES") return GBC_SOLVER_FGMRES;
+      if (s == "FGMRES" || s == "GCR") return GBC_SOLVER_FGMRES;  // both minimise over a flexible Krylov space
+      if (s == "BICGSTAB") return GBC_SOLVER_BICGSTAB;
       return GBC_SOLVER_MIXED;
     }
     // canonical site index s = x + Lx*(y + Ly*(z + Lz*t)) -> QDP++ linear index on this node

@@ -64,6 +64,9 @@ extern "C" {
                                      (inv_multiprec_richardson.cc:13-107)                            */
 #define GBC_SOLVER_FGMRES 3       /* FGMRESDR_INVERTER with NDefl = 0 (syssolver_linop_fgmres_dr.cc),
                                      preconditioned by the learned network when loaded               */
+#define GBC_SOLVER_BICGSTAB 4     /* FP64 defect correction around a reliable BiCGStab on M~ in the
+                                     sloppy precision: RELIABLE_BICGSTAB_MP_CLOVER_INVERTER
+                                     (reliable_bicgstab.cc:93-277), QUDA SolverType BICGSTAB        */
 /* linear systems */
 #define GBC_SYS_MEO 0    /* M~ psi_o = chi_o           (LinOpSystemSolver, syssolver_linop.h)          */
 #define GBC_SYS_MDAGM 1  /* M~^dag M~ psi_o = chi_o    (MdagMSystemSolver, syssolver_mdagm.h:25-35)    */

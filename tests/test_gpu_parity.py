@@ -121,8 +121,11 @@ def _true_rel(op, psi, chi):
 @pytest.mark.parametrize("solver,sloppy", [(G.SOLVER_CG, 0), (G.SOLVER_MIXED, G.PREC_HALF),
                                            (G.SOLVER_MIXED, G.PREC_SINGLE), (G.SOLVER_RELIABLE_CG, G.PREC_HALF),
                                            (G.SOLVER_RELIABLE_CG, G.PREC_SINGLE), (G.SOLVER_FGMRES, G.PREC_HALF),
-                                           (G.SOLVER_FGMRES, G.PREC_SINGLE), (G.SOLVER_FGMRES, G.PREC_DOUBLE)],
-                         ids=["cg64", "mixed16", "mixed32", "rel16", "rel32", "fgmres16", "fgmres32", "fgmres64"])
+                                           (G.SOLVER_FGMRES, G.PREC_SINGLE), (G.SOLVER_FGMRES, G.PREC_DOUBLE),
+                                           (G.SOLVER_BICGSTAB, G.PREC_HALF), (G.SOLVER_BICGSTAB, G.PREC_SINGLE),
+                                           (G.SOLVER_BICGSTAB, G.PREC_DOUBLE)],
+                         ids=["cg64", "mixed16", "mixed32", "rel16", "rel32", "fgmres16", "fgmres32", "fgmres64",
+                              "bicgstab16", "bicgstab32", "bicgstab64"])
 def test_solvers_reach_1e10(setup, solver, sloppy):
     from oracle import oracle as O
     dims, op, ctx = setup
