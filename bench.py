@@ -5,6 +5,10 @@ U = reunit(exp(i 0.3 H)) (seeded), kappa = 0.1250, c_sw = 1.6, the 12 spin-colou
 at the origin solved together as one multi-RHS batch through the full even-odd system
 (Schur prep, odd solve, even reconstruction: Chroma's PrecFermActQprop + quarkProp4_a).
 
+The solve is the FP64 defect correction around a reliable BiCGStab on the even-odd operator M~
+with the FP16 stencil (SolverType BICGSTAB); the same solve with the inner CGNE and an FP64
+BiCGStab are reported beside it.
+
 A step is one such propagator solve.  value = seconds per propagator (device-resident inputs,
 CUDA events on the library stream, max over ranks / N for N replicas); e2e = the same through
 gbc_solve with pinned host buffers (H2D of the sources and D2H of the solution inside the clock).
@@ -32,6 +36,7 @@ METRIC = "Solve time at rel. residual 1e-10: learned+mixed vs plain CG; Dslash H
 DIMS = (32, 32, 32, 64)
 KAPPA, CSW, EPS, SEED = 0.1250, 1.6, 0.3, 20251203
 RSD = 1e-10
+DELTA = 0.01  # reliable-update threshold of the inner BiCGStab (the XML's Delta)
 # InvCG2 iterations of one source of this workload (FP64 CGNE; the GPU FP64 CG and the oracle run
 # the same recursion).  The GPU arm re-measures it every run and reports both.
 CG_ITERS_REF = 120
@@ -192,7 +197,7 @@ WEIGHTS = os.path.join(ROOT, "chroma_gb300", "weights", "cnn_16x16x16x32_k0.115_
 def side_workloads(G):
     """The smaller configurations, each reported beside the headline (not part of `value`):
     - stout16: 16^3x32, eps 0.2 + 4 stout steps rho 0.1, kappa 0.12, c_sw 1.2, one Gaussian source:
-      mixed FP16/FP64 vs plain FP64 CG on the same GPU;
+      mixed FP16/FP64 (inner CGNE and inner BiCGStab) vs plain FP64 CG on the same GPU;
     - uneven_batch: 8^3x16, 12^3x24, 16^3x32, 20^3x40 (kappa 0.124, c_sw 1.5, one Z2 source each)
       solved as one batch (one multi-lattice stencil launch per application) vs one by one;
     - learned16: 16^3x32, kappa 0.115, c_sw 1.0, FGMRES(16) with and without the trained network on
@@ -206,7 +211,8 @@ def side_workloads(G):
     ctx.load_gauge(u)
     chi = S.gaussian(dims, 17, cb=1).reshape(1, -1, 12)
     rec = {}
-    for name, kw in (("mixed_fp16", dict(solver=G.SOLVER_MIXED)), ("plain_fp64_cg", dict(solver=G.SOLVER_CG))):
+    for name, kw in (("mixed_fp16", dict(solver=G.SOLVER_MIXED)), ("mixed_fp16_bicgstab", dict(solver=G.SOLVER_BICGSTAB)),
+                     ("plain_fp64_cg", dict(solver=G.SOLVER_CG))):
         ctx.solve(chi, rsd_target=RSD, **kw)  # warm-up (tuning, workspaces)
         ts = []
         for _ in range(3):
@@ -215,6 +221,7 @@ def side_workloads(G):
         rec[name] = {"seconds": statistics.median(ts), "iterations": res[0]["n_count"],
                      "true_rel_resid": res[0]["rel_resid"]}
     rec["speedup"] = rec["plain_fp64_cg"]["seconds"] / rec["mixed_fp16"]["seconds"]
+    rec["speedup_bicgstab"] = rec["plain_fp64_cg"]["seconds"] / rec["mixed_fp16_bicgstab"]["seconds"]
     out["stout16"] = rec
     ctx.close()
     # uneven lattices
@@ -325,7 +332,9 @@ def main():
     # device-resident sources / solutions in the canonical layout
     chi_d = torch.from_numpy(src.view(np.float64)).cuda()
     psi_d = torch.zeros_like(chi_d)
-    solve_kw = dict(solver=G.SOLVER_MIXED, system=G.SYS_FULL, rsd_target=RSD, sloppy_precision=G.PREC_HALF)
+    # Delta 0.01: a reliable update (FP32 operator) each time the iterated residual fell by 100x
+    solve_kw = dict(solver=G.SOLVER_BICGSTAB, system=G.SYS_FULL, rsd_target=RSD, sloppy_precision=G.PREC_HALF,
+                    delta=DELTA)
 
     def step():
         res, rc = ctx.solve_device(psi_d.data_ptr(), chi_d.data_ptr(), nsrc, **solve_kw)
@@ -381,6 +390,20 @@ def main():
         ref0 = psi_cg.cpu().numpy().view(np.complex128).reshape(V, 12)
         err_vs_fp64 = float(np.linalg.norm(psi_host[0] - ref0) / np.linalg.norm(ref0))
 
+    # the same solve with the inner CGNE, and FP64 BiCGStab (12-RHS batch, FP64 defect correction
+    # around an FP64 inner BiCGStab): context for the choice of the inner solver
+    inner_cgne, plain_bicg = None, None
+    if args.plain_steps > 0:
+        psi1 = torch.zeros_like(chi_d)
+        for _ in range(2):  # the first one tunes the stencil variants that only CGNE uses
+            res, rc = ctx.solve_device(psi1.data_ptr(), chi_d.data_ptr(), nsrc, **dict(solve_kw, solver=G.SOLVER_MIXED, delta=0.1))
+        inner_cgne = {"seconds": res[0]["device_seconds"], "inner_iterations_per_rhs": res[0]["n_count"],
+                      "true_rel_resid_max": max(r["rel_resid"] for r in res), "rc": rc}
+        res, rc = ctx.solve_device(psi1.data_ptr(), chi_d.data_ptr(), nsrc,
+                                   **dict(solve_kw, sloppy_precision=G.PREC_DOUBLE))
+        plain_bicg = {"seconds": res[0]["device_seconds"], "iterations_per_rhs": res[0]["n_count"],
+                      "true_rel_resid_max": max(r["rel_resid"] for r in res), "rc": rc}
+
     # Dslash roofline: the FP16 12-RHS hopping kernel (dominant), cold L2 per launch
     pk, pk_kind = peaks()
     sec, byts = ctx.time_operator(G.OP_DSLASH, G.PREC_HALF, nrhs=12, iters=20, flush_l2=True)
@@ -408,7 +431,7 @@ def main():
     psi_h = torch.zeros_like(chi_h).pin_memory()
     e2e_t = []
     import ctypes as C
-    p = G.SolveParams(G.SOLVER_MIXED, G.SYS_FULL, RSD, 10000, 0.1, 10.0, G.PREC_HALF, 0.0, 0, 16, 0, 1)
+    p = G.SolveParams(G.SOLVER_BICGSTAB, G.SYS_FULL, RSD, 10000, DELTA, 10.0, G.PREC_HALF, 0.0, 0, 16, 0, 1)
     for i in range(max(1, min(args.steps, 3))):
         res_arr = (G.Result * nsrc)()
         t0 = time.perf_counter()
@@ -435,12 +458,14 @@ def main():
         "config": {"workload": f"{'x'.join(map(str, dims))} Wilson-clover propagator, 12 point sources, "
                                f"kappa={KAPPA}, c_sw={CSW}, hot start eps={EPS}, antiperiodic t, full system, "
                                f"FP64 true residual {RSD}",
-                   "solver": "FP64 defect correction + reliable-update CGNE (FP16 stencil, 12-real links), "
-                             "12-RHS batch",
+                   "solver": "FP64 defect correction + reliable-update BiCGStab on M~ (FP16 stencil, "
+                             f"12-real links, Delta {DELTA}), 12-RHS batch",
                    "l2": "256 MiB L2 flush between timed steps; the fields exceed L2",
                    "parallelism": f"replicas x{world}"},
         "plain_cg_fp64_s": plain, "speedup_vs_plain_cg": plain / value if (value and plain) else None,
         "iterations": {"mixed_inner_per_rhs_median": int(np.median(iters)), "plain_cg_per_rhs": plain_iters},
+        "same_solve_inner_cgne": inner_cgne,
+        "plain_bicgstab_fp64_batched": plain_bicg,
         "true_rel_resid_max": max(r["rel_resid"] for r in last),
         "plain_cg_true_rel_resid_max": max(plain_res) if plain else None,
         "rel_error_vs_fp64_cg_src0": err_vs_fp64,

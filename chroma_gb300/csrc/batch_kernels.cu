@@ -69,9 +69,9 @@ __global__ void __launch_bounds__(kSites) update_kernel(const LatCg* lat, const 
   const int2 w = work[blockIdx.x];
   const LatCg& l = lat[w.x];
   const int idx = w.y * kSites + threadIdx.x;
-  double acc = 0.0;
+  using T = typename PA::real;
+  T acc = 0;  // site and warp sums in the compute precision, block sums in FP64
   if (idx < l.Vh) {
-    using T = typename PA::real;
     cplx<T> es[12], rs[12];
     cplx<typename PO::real> ps[12], qs[12];
     ldf<PA>(es, l.e, idx);
@@ -90,12 +90,12 @@ __global__ void __launch_bounds__(kSites) update_kernel(const LatCg* lat, const 
     }
     stf<PA>(l.e, idx, es);
     stf<PA>(l.r, idx, rs);
-    acc = (double)s;
+    acc = s;
   }
   __shared__ double sh[kSites / 32];
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)acc;
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;

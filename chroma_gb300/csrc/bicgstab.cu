@@ -7,7 +7,8 @@
 //   p = r + beta (p - omega v)
 //
 // The operator and the vectors it reads (p, v, s, t) are in the sloppy precision; x, r and the
-// shadow r0 in the accumulator precision.  x and r are updated from the accumulator-precision r of
+// shadow residual r0 in the accumulator precision (an fp16 r0 made the iteration counts of the
+// right-hand sides spread and cost more reliable updates than its bandwidth saved).  x and r are updated from the accumulator-precision r of
 // the step before (x += alpha p + omega (r - alpha v), r -= alpha v + omega t), so the sloppy copy
 // of s only feeds the operator and the (t, s) product.  Every scalar lives on the device (one thread
 // per right-hand side), so iterations replay from CUDA graphs; the host looks at the scalars every
@@ -50,22 +51,75 @@ __device__ __forceinline__ void stv(const Spinor& f, int idx, int r, const cplx<
                   f.stride, x);
 }
 
-// grid-stride site loop, one y-block row per right-hand side, NRED sums per right-hand side
-template <int NRED, class F>
-__global__ void __launch_bounds__(BT) bi_site_kernel(int Vh, F f, double* partials, int part_stride, int nrhs) {
-  const int r = blockIdx.y;
-  double acc[NRED > 0 ? NRED : 1];
+// complex components 4c .. 4c + 3 of right-hand side r at site idx; n = the site norm of an fp16
+// field (ignored otherwise)
+template <typename P>
+__device__ __forceinline__ void ld4(cplx<typename P::real> (&x)[4], const Spinor& f, int idx, int r, int c, float n) {
+  const char* base = (const char*)f.v + (size_t)r * f.rhs_bytes;
+  if constexpr (std::is_same<P, PrecD>::value) {
+    const double2* p = reinterpret_cast<const double2*>(base);
 #pragma unroll
-  for (int q = 0; q < (NRED > 0 ? NRED : 1); ++q) acc[q] = 0.0;
+    for (int q = 0; q < 4; ++q) {
+      const double2 v = ldg(p + (size_t)(4 * c + q) * f.stride + idx);
+      x[q] = {v.x, v.y};
+    }
+  } else if constexpr (std::is_same<P, PrecS>::value) {
+    const float4* p = reinterpret_cast<const float4*>(base);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const float4 v = ldg(p + (size_t)(2 * c + h) * f.stride + idx);
+      x[2 * h] = {v.x, v.y};
+      x[2 * h + 1] = {v.z, v.w};
+    }
+  } else {
+    const uint4 v = ldg(reinterpret_cast<const uint4*>(base) + (size_t)c * f.stride + idx);
+    const float2 a = h2f(v.x), b = h2f(v.y), d = h2f(v.z), e = h2f(v.w);
+    x[0] = {a.x * n, a.y * n};
+    x[1] = {b.x * n, b.y * n};
+    x[2] = {d.x * n, d.y * n};
+    x[3] = {e.x * n, e.y * n};
+  }
+}
+// store components 4c .. 4c + 3 (FP64 / FP32 fields only: an fp16 site needs all 12 for its norm)
+template <typename P>
+__device__ __forceinline__ void st4(const Spinor& f, int idx, int r, int c, const cplx<typename P::real> (&x)[4]) {
+  static_assert(!std::is_same<P, PrecH>::value, "fp16 stores go through store_spinor");
+  char* base = (char*)f.v + (size_t)r * f.rhs_bytes;
+  if constexpr (std::is_same<P, PrecD>::value) {
+    double2* p = reinterpret_cast<double2*>(base);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) p[(size_t)(4 * c + q) * f.stride + idx] = make_double2(x[q].re, x[q].im);
+  } else {
+    float4* p = reinterpret_cast<float4*>(base);
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      p[(size_t)(2 * c + h) * f.stride + idx] = make_float4(x[2 * h].re, x[2 * h].im, x[2 * h + 1].re, x[2 * h + 1].im);
+  }
+}
+template <typename P>
+__device__ __forceinline__ float site_norm(const Spinor& f, int idx, int r) {
+  if constexpr (std::is_same<P, PrecH>::value) return ldg(f.norm + (size_t)r * f.norm_rhs_stride + idx);
+  return 1.0f;
+}
+
+// grid-stride site loop, one y-block row per right-hand side, NRED sums per right-hand side
+// F::kMinb resident blocks per SM: 4 (64 registers) for the FP32 accumulators, 2 for FP64
+template <int NRED, class F>
+__global__ void __launch_bounds__(BT, F::kMinb) bi_site_kernel(int Vh, F f, double* partials, int part_stride, int nrhs) {
+  using A = typename AccOf<F>::type;  // thread and warp sums in the compute precision
+  const int r = blockIdx.y;
+  A acc[NRED > 0 ? NRED : 1];
+#pragma unroll
+  for (int q = 0; q < (NRED > 0 ? NRED : 1); ++q) acc[q] = 0;
   for (int idx = blockIdx.x * BT + threadIdx.x; idx < Vh; idx += gridDim.x * BT) f(idx, r, acc);
   if constexpr (NRED > 0) {
     __shared__ double sh[NRED][BT / 32];
 #pragma unroll
     for (int q = 0; q < NRED; ++q) {
-      double v = acc[q];
+      A v = acc[q];
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-      if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = v;
+      if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = (double)v;
     }
     __syncthreads();
     if (threadIdx.x < NRED) {
@@ -80,6 +134,7 @@ __global__ void __launch_bounds__(BT) bi_site_kernel(int Vh, F f, double* partia
 // s = r - alpha v
 template <typename PA, typename PO>
 struct SUpdF {
+  static constexpr int kMinb = std::is_same<PA, PrecD>::value ? 2 : 4;
   const BiScal* sc;
   Spinor r, v, s;
   __device__ void operator()(int idx, int k, double*) const {
@@ -99,8 +154,10 @@ struct SUpdF {
 // (t, s) and |t|^2
 template <typename PO>
 struct TsTtF {
+  static constexpr int kMinb = std::is_same<PO, PrecD>::value ? 2 : 4;
+  using Acc = typename PO::real;
   Spinor t, s;
-  __device__ void operator()(int idx, int k, double* acc) const {
+  __device__ void operator()(int idx, int k, Acc* acc) const {
     using T = typename PO::real;
     cplx<T> ts[12], ss[12];
     ldv<PO>(ts, t, idx, k);
@@ -112,51 +169,63 @@ struct TsTtF {
       im = fmadd(ts[q].re, ss[q].im, fmadd(-ts[q].im, ss[q].re, im));
       tt = fmadd(ts[q].re, ts[q].re, fmadd(ts[q].im, ts[q].im, tt));
     }
-    acc[0] += (double)re;
-    acc[1] += (double)im;
-    acc[2] += (double)tt;
+    acc[0] += re;
+    acc[1] += im;
+    acc[2] += tt;
   }
 };
 
-// x += alpha p + omega (r - alpha v);  r -= alpha v + omega t;  |r|^2 and (r0, r)
+// x += alpha p + omega (r - alpha v);  r -= alpha v + omega t;  |r|^2 and (r0, r).  Six vectors
+// in and two out per site: processed four colour-spin components at a time (a whole site of all
+// eight would hold ~150 registers and leave one block per SM for a bandwidth-bound loop).
 template <typename PA, typename PO>
 struct XRUpdF {
+  static constexpr int kMinb = std::is_same<PA, PrecD>::value ? 2 : 4;
+  using Acc = typename PA::real;
   const BiScal* sc;
   Spinor x, r, p, v, t, r0;
-  __device__ void operator()(int idx, int k, double* acc) const {
+  __device__ void operator()(int idx, int k, Acc* acc) const {
     using T = typename PA::real;
-    cplx<T> xs[12], rs[12], hs[12];
-    cplx<typename PO::real> ps[12], vs[12], ts[12];
-    ldv<PA>(xs, x, idx, k);
-    ldv<PA>(rs, r, idx, k);
-    ldv<PA>(hs, r0, idx, k);
-    ldv<PO>(ps, p, idx, k);
-    ldv<PO>(vs, v, idx, k);
-    ldv<PO>(ts, t, idx, k);
+    using U = typename PO::real;
+    const float np = site_norm<PO>(p, idx, k), nv = site_norm<PO>(v, idx, k), nt = site_norm<PO>(t, idx, k);
+    const float nh = site_norm<PA>(r0, idx, k);
     const double2 al = sc[k].alpha, om = sc[k].omega;
     const cplx<T> a{(T)al.x, (T)al.y}, w{(T)om.x, (T)om.y};
     T rr = 0, re = 0, im = 0;
+#pragma unroll 1
+    for (int c = 0; c < 3; ++c) {
+      cplx<T> xs[4], rs[4], hs[4];
+      cplx<U> ps[4], vs[4], ts[4];
+      ld4<PA>(xs, x, idx, k, c, 1.f);
+      ld4<PA>(rs, r, idx, k, c, 1.f);
+      ld4<PA>(hs, r0, idx, k, c, nh);
+      ld4<PO>(ps, p, idx, k, c, np);
+      ld4<PO>(vs, v, idx, k, c, nv);
+      ld4<PO>(ts, t, idx, k, c, nt);
 #pragma unroll
-    for (int q = 0; q < 12; ++q) {
-      const cplx<T> pq{(T)ps[q].re, (T)ps[q].im}, vq{(T)vs[q].re, (T)vs[q].im}, tq{(T)ts[q].re, (T)ts[q].im};
-      const cplx<T> sq = rs[q] - a * vq;
-      xs[q] = xs[q] + a * pq + w * sq;
-      rs[q] = sq - w * tq;
-      rr = fmadd(rs[q].re, rs[q].re, fmadd(rs[q].im, rs[q].im, rr));
-      re = fmadd(hs[q].re, rs[q].re, fmadd(hs[q].im, rs[q].im, re));
-      im = fmadd(hs[q].re, rs[q].im, fmadd(-hs[q].im, rs[q].re, im));
+      for (int q = 0; q < 4; ++q) {
+        const cplx<T> pq{(T)ps[q].re, (T)ps[q].im}, vq{(T)vs[q].re, (T)vs[q].im}, tq{(T)ts[q].re, (T)ts[q].im};
+        const cplx<T> hq = hs[q];
+        const cplx<T> sq = rs[q] - a * vq;
+        xs[q] = xs[q] + a * pq + w * sq;
+        rs[q] = sq - w * tq;
+        rr = fmadd(rs[q].re, rs[q].re, fmadd(rs[q].im, rs[q].im, rr));
+        re = fmadd(hq.re, rs[q].re, fmadd(hq.im, rs[q].im, re));
+        im = fmadd(hq.re, rs[q].im, fmadd(-hq.im, rs[q].re, im));
+      }
+      st4<PA>(x, idx, k, c, xs);
+      st4<PA>(r, idx, k, c, rs);
     }
-    stv<PA>(x, idx, k, xs);
-    stv<PA>(r, idx, k, rs);
-    acc[0] += (double)rr;
-    acc[1] += (double)re;
-    acc[2] += (double)im;
+    acc[0] += rr;
+    acc[1] += re;
+    acc[2] += im;
   }
 };
 
 // p = r + beta (p - omega v)
 template <typename PA, typename PO>
 struct PUpdF {
+  static constexpr int kMinb = std::is_same<PA, PrecD>::value ? 2 : 4;
   const BiScal* sc;
   Spinor r, p, v;
   __device__ void operator()(int idx, int k, double*) const {
@@ -283,10 +352,14 @@ InnerStats bicgstab(gbc_ctx* c, int pa, int po, double tol, int maxit, double de
   blas_copy(g, r0, b, st);
   blas_copy(g, p, b, st);
   blas_norm2(g, b, red(c), st);
-  std::vector<double> bb(n);
+  std::vector<double> bb(n), rho0(2 * n);
   GBC_CUDA(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
   sync(c);
   std::memcpy(bb.data(), c->h_result, sizeof(double) * n);
+  blas_cdot(g, r0, r, red(c), st);  // rho = (r0, r)
+  GBC_CUDA(cudaMemcpyAsync(c->h_result, c->d_result, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, st));
+  sync(c);
+  std::memcpy(rho0.data(), c->h_result, sizeof(double) * 2 * n);
 
   // device scalars: kept in the context (no allocation inside the outer loop)
   if (c->bisc_cap < n) {
@@ -304,7 +377,7 @@ InnerStats bicgstab(gbc_ctx* c, int pa, int po, double tol, int maxit, double de
   for (int i = 0; i < n; ++i) {
     BiScal& q = hs[i];
     std::memset(&q, 0, sizeof(q));
-    q.rho = make_double2(bb[i], 0.0);
+    q.rho = make_double2(rho0[i], rho0[n + i]);
     q.rr = bb[i];
     q.rsd_sq = tol * tol * bb[i];
     q.status = std::isfinite(bb[i]) ? GBC_OK : GBC_ERR_NONFINITE;

@@ -13,19 +13,20 @@ constexpr int BLAS_THREADS = 256;
 // grid-stride driver: f(idx, rhs, acc) per site; NRED doubles reduced per right-hand side
 template <int NRED, class F>
 __global__ void __launch_bounds__(BLAS_THREADS) site_kernel(int Vh, F f, double* partials, int part_stride, int nrhs) {
+  using A = typename AccOf<F>::type;
   const int r = blockIdx.y;
-  double acc[NRED > 0 ? NRED : 1];
+  A acc[NRED > 0 ? NRED : 1];
 #pragma unroll
-  for (int q = 0; q < (NRED > 0 ? NRED : 1); ++q) acc[q] = 0.0;
+  for (int q = 0; q < (NRED > 0 ? NRED : 1); ++q) acc[q] = 0;
   for (int idx = blockIdx.x * BLAS_THREADS + threadIdx.x; idx < Vh; idx += gridDim.x * BLAS_THREADS) f(idx, r, acc);
   if constexpr (NRED > 0) {
     __shared__ double sh[NRED][BLAS_THREADS / 32];
 #pragma unroll
     for (int q = 0; q < NRED; ++q) {
-      double v = acc[q];
+      A v = acc[q];
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-      if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = v;
+      if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = (double)v;
     }
     __syncthreads();
     if (threadIdx.x < NRED) {
@@ -74,37 +75,38 @@ struct ZeroF {
 
 template <typename P>
 struct Norm2F {
+  using Acc = typename P::real;  // site and thread sums in the field's compute precision
   Spinor x;
-  __device__ void operator()(int idx, int r, double* acc) const {
+  __device__ void operator()(int idx, int r, Acc* acc) const {
     cplx<typename P::real> a[12];
     ld<P>(a, x, idx, r);
-    // site sums in the field's compute precision, running sums in FP64
     using T = typename P::real;
     T s = 0;
 #pragma unroll
     for (int k = 0; k < 12; ++k) s = fmadd(a[k].re, a[k].re, fmadd(a[k].im, a[k].im, s));
-    acc[0] += (double)s;
+    acc[0] += s;
   }
 };
 
 template <typename PX, typename PY>
 struct CdotF {
+  using Acc = typename std::conditional<std::is_same<PX, PrecD>::value || std::is_same<PY, PrecD>::value, double,
+                                        float>::type;
   Spinor x, y;
-  __device__ void operator()(int idx, int r, double* acc) const {
+  __device__ void operator()(int idx, int r, Acc* acc) const {
     cplx<typename PX::real> a[12];
     cplx<typename PY::real> b[12];
     ld<PX>(a, x, idx, r);
     ld<PY>(b, y, idx, r);
-    using T = typename std::conditional<std::is_same<PX, PrecD>::value || std::is_same<PY, PrecD>::value, double,
-                                        float>::type;
+    using T = Acc;
     T re = 0, im = 0;
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
       re = fmadd((T)a[k].re, (T)b[k].re, fmadd((T)a[k].im, (T)b[k].im, re));
       im = fmadd((T)a[k].re, (T)b[k].im, fmadd(-(T)a[k].im, (T)b[k].re, im));
     }
-    acc[0] += (double)re;
-    acc[1] += (double)im;
+    acc[0] += re;
+    acc[1] += im;
   }
 };
 
@@ -134,9 +136,10 @@ struct AxpbyF {
 // x += a p; r -= a q; acc = |r|^2   (x, r in PA;  p, q in PO)
 template <typename PA, typename PO>
 struct CgUpdateF {
+  using Acc = typename PA::real;
   const double* a;
   Spinor x, p, r, q;
-  __device__ void operator()(int idx, int rr, double* acc) const {
+  __device__ void operator()(int idx, int rr, Acc* acc) const {
     using T = typename PA::real;
     cplx<T> xs[12], rs[12];
     cplx<typename PO::real> ps[12], qs[12];
@@ -156,7 +159,7 @@ struct CgUpdateF {
     }
     st<PA>(x, idx, rr, xs);
     st<PA>(r, idx, rr, rs);
-    acc[0] += (double)s;
+    acc[0] += s;
   }
 };
 
@@ -184,8 +187,9 @@ struct XpayF {
 // y = x - y; acc = |y|^2
 template <typename P>
 struct XmyNormF {
+  using Acc = typename P::real;
   Spinor x, y;
-  __device__ void operator()(int idx, int r, double* acc) const {
+  __device__ void operator()(int idx, int r, Acc* acc) const {
     cplx<typename P::real> xs[12], ys[12];
     ld<P>(xs, x, idx, r);
     ld<P>(ys, y, idx, r);
@@ -196,7 +200,7 @@ struct XmyNormF {
       s = fmadd(ys[k].re, ys[k].re, fmadd(ys[k].im, ys[k].im, s));
     }
     st<P>(y, idx, r, ys);
-    acc[0] += (double)s;
+    acc[0] += s;
   }
 };
 

@@ -189,7 +189,7 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce
     float best_ms = 1e30f;
     for (int si = 0; si < kNumHopShapes; ++si) {
       const HopShape sh = kHopShapes[si];
-      if (!hop_shape_valid(sh, prec, h.nrhs, h.g.L[3])) continue;
+      if (!hop_shape_valid(sh, prec, h.nrhs, h.g.L[3]) || hop_blocks(sh, h.g.Vh) > h.part_stride) continue;
       if (hop_launch(prec, recon, mode, dag, reduce, h, sh, c->stream) < 0) continue;
       if (cudaPeekAtLastError() != cudaSuccess) {
         cudaGetLastError();  // e.g. too many resources for this shape: not a candidate
@@ -248,10 +248,10 @@ void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, con
   h.partials = c->d_partials;
   h.part_stride = c->part_stride;
   const HopShape sh = kHopShapes[tuned_shape(c, prec, f.recon, mode, dag, reduce, h)];
+  if (hop_blocks(sh, h.g.Vh) > c->part_stride) throw std::string("partials buffer too small");
   int nb = hop_launch(prec, f.recon, mode, dag, reduce, h, sh, c->stream);
   if (nb < 0) throw std::string("hopping kernel variant not compiled");
   count_launch();
-  if (nb > c->part_stride) throw std::string("partials buffer too small");
   GBC_CUDA(cudaGetLastError());
   if (reduce) reduce_finalize(red(c), 1, in.nrhs, nb, c->stream);
 }
@@ -386,8 +386,8 @@ int gbc_create(gbc_ctx** out, const gbc_geom* geom, const gbc_action* act, const
         if (m != act->t_dir) c->link_coeff[m] = act->nu / act->xi_0;
     }
     GBC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-    // reduction partials: the largest grid is the hopping kernel with 32 sites per block
-    c->part_stride = (g.Vh + 31) / 32;
+    // reduction partials: the largest grid is the hopping kernel with 16 sites per block
+    c->part_stride = (g.Vh + 15) / 16;
     if (c->part_stride < blas_blocks(g)) c->part_stride = blas_blocks(g);
     GBC_CUDA(cudaMalloc(&c->d_partials, sizeof(double) * 3 * c->max_rhs * (size_t)c->part_stride));
     GBC_CUDA(cudaMalloc(&c->d_result, sizeof(double) * 3 * c->max_rhs));

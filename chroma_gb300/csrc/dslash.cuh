@@ -533,7 +533,8 @@ __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group
     stage_links<P, RECON, TX>(lsm, a, sblock);
     __syncthreads();
   }
-  double local = 0.0;
+  // |out|^2: thread and warp sums in the compute precision, block sums in FP64
+  T local = 0;
   if (active) {
     Coord c = cb_coords(g, idx, a.out_parity);
     const char* in = (const char*)a.in + (size_t)rhs * a.in_rhs_bytes;
@@ -565,14 +566,14 @@ __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group
       hop_dir<P, RECON, 2, DAG>(acc, a, c, idx, in, in_norm);
       hop_dir<P, RECON, 3, DAG>(acc, a, c, idx, in, in_norm);
     }
-    local = (double)hop_epilogue<P, MODE, DAG, REDUCE>(a, rhs, idx, acc);
+    local = hop_epilogue<P, MODE, DAG, REDUCE>(a, rhs, idx, acc);
   }
   if constexpr (REDUCE) {
     // warps never straddle two right-hand sides (TX is a multiple of 32)
     __shared__ double wsum[TX * NRB / 32];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
-    if ((tid & 31) == 0) wsum[tid >> 5] = local;
+    if ((tid & 31) == 0) wsum[tid >> 5] = (double)local;
     __syncthreads();
     if (tid < NRB) {
       const int r = group * NRB + tid;
@@ -772,7 +773,7 @@ __global__ void __launch_bounds__(TX, MINB) hop_kernel_pair(const HopArgs a) {
   const Geom& g = a.g;
   const int half = g.Vh >> 1;
   const int ia = sblock * TX + threadIdx.x;
-  double local = 0.0;
+  float local = 0.f;  // thread and warp sums in FP32, block sums in FP64
   if (ia < half) {
     const int ib = ia + half;
     const Coord ca = cb_coords(g, ia, a.out_parity);
@@ -794,14 +795,14 @@ __global__ void __launch_bounds__(TX, MINB) hop_kernel_pair(const HopArgs a) {
       sa[k] = {acc[k].r.x, acc[k].i.x};
       sb[k] = {acc[k].r.y, acc[k].i.y};
     }
-    local = (double)hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, ia, sa);
-    local += (double)hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, ib, sb);
+    local = hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, ia, sa);
+    local += hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, ib, sb);
   }
   if constexpr (REDUCE) {
     __shared__ double wsum[TX / 32];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = local;
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)local;
     __syncthreads();
     if (threadIdx.x == 0) {
       double s = 0.0;

@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(TX, MINB) hop_kernel_async(const HopArgs a) {
   const int rhs = blockIdx.x - sblock * a.nrhs;
   const Geom& g = a.g;
   const int idx = sblock * TX + threadIdx.x;
-  double local = 0.0;
+  float local = 0.f;  // thread and warp sums in FP32, block sums in FP64
   if (idx < g.Vh) {
     const Coord c = cb_coords(g, idx, a.out_parity);
     const HopSites hs = hop_sites(g, c);
@@ -167,13 +167,13 @@ __global__ void __launch_bounds__(TX, MINB) hop_kernel_async(const HopArgs a) {
     cplx<float> out[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) out[k] = {acc[k].x, acc[k].y};
-    local = (double)hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, idx, out);
+    local = hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, idx, out);
   }
   if constexpr (REDUCE) {
     __shared__ double wsum[TX / 32];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = local;
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)local;
     __syncthreads();
     if (threadIdx.x == 0) {
       double s = 0.0;

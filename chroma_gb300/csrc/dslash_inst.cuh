@@ -4,6 +4,7 @@
 #pragma once
 #include "dslash.cuh"
 #include "dslash_async.cuh"
+#include "dslash_rpair.cuh"
 
 namespace gbc {
 
@@ -26,6 +27,22 @@ static int hop_shape(const HopArgs& a, HopShape sh, cudaStream_t s) {
   GBC_SHAPE(32, 12, 2)
 #undef GBC_SHAPE
   if constexpr (std::is_same<P, PrecH>::value) {
+    if (sh.pair == 3) {
+      // two right-hand sides per thread: blocks of TS sites x NRB right-hand sides, TS NRB / 2 threads
+      if (a.nrhs & 1) return -1;
+#define GBC_RPAIR(TS, NRB, MINB)                                                          \
+  if (sh.tx == TS && sh.nrb == NRB && sh.minb == MINB) {                                  \
+    const int ng = (a.nrhs + NRB - 1) / NRB;                                              \
+    hop_kernel_rp<RECON, MODE, DAG, REDUCE, TS, NRB, MINB><<<(unsigned)(nbx * ng), TS * NRB / 2, 0, s>>>(a); \
+    return nbx;                                                                           \
+  }
+      GBC_RPAIR(32, 12, 2)
+      GBC_RPAIR(16, 12, 5)
+      GBC_RPAIR(16, 12, 4)
+      GBC_RPAIR(16, 4, 10)
+#undef GBC_RPAIR
+      return -1;
+    }
     if (sh.nrb != 1) return -1;
     if (sh.pair == 1) {
       // two sites per thread: blocks of TX threads cover 2 TX sites

@@ -103,6 +103,19 @@ struct PrecD { using real = double; static constexpr int bytes = 8; };
 struct PrecS { using real = float; static constexpr int bytes = 4; };
 struct PrecH { using real = float; static constexpr int bytes = 2; };  // fp16 storage, fp32 arithmetic
 
+// Accumulator of a site functor's reductions: F::Acc when the functor declares one (its compute
+// precision), else double.  The reduction drivers sum a thread's sites and the lanes of a warp in
+// Acc and only the per-warp results in FP64: GB300's FP64 pipe is slow enough that one FP64
+// conversion and add per site and quantity made a bandwidth-bound reduction FP64-bound.
+template <class F, class = void>
+struct AccOf {
+  using type = double;
+};
+template <class F>
+struct AccOf<F, std::void_t<typename F::Acc>> {
+  using type = typename F::Acc;
+};
+
 template <typename P> struct Store;
 template <> struct Store<PrecD> { using vec = double2; };
 template <> struct Store<PrecS> { using vec = float4; };

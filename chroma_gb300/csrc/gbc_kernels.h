@@ -58,7 +58,9 @@ struct HopArgs {
 // Launch geometry chosen by the caller (autotuned): TX sites x NRB right-hand sides per block,
 // MINB resident blocks per SM requested from the register allocator.  pair = 1: the fp16 kernel
 // with two sites per thread (TX threads cover 2 TX sites; fp16 storage and even Lt only);
-// pair = 2: the fp16 kernel that streams the next hops through a shared-memory ring (cp.async).
+// pair = 2: the fp16 kernel that streams the next hops through a shared-memory ring (cp.async);
+// pair = 3: the fp16 kernel with two right-hand sides per thread (TX sites x NRB right-hand sides,
+// TX NRB / 2 threads; even nrhs only).
 struct HopShape {
   int tx;
   int nrb;
@@ -68,14 +70,22 @@ struct HopShape {
 // the compiled candidates (dslash_inst.cuh)
 constexpr HopShape kHopShapes[] = {{128, 1, 1, 0}, {128, 1, 6, 0}, {32, 4, 1, 0},  {32, 4, 5, 0},
                                    {64, 2, 4, 0},  {32, 12, 2, 0}, {128, 1, 2, 1}, {128, 1, 3, 1},
-                                   {64, 1, 6, 1},  {128, 1, 3, 2}, {128, 1, 4, 2}, {64, 1, 8, 2}};
-constexpr int kNumHopShapes = 12;
+                                   {64, 1, 6, 1},  {128, 1, 3, 2}, {128, 1, 4, 2}, {64, 1, 8, 2},
+                                   {32, 12, 2, 3}, {16, 12, 5, 3}, {16, 12, 4, 3}, {16, 4, 10, 3}};
+constexpr int kNumHopShapes = 16;
 // whether shape sh can run the hopping term of precision prec over nrhs right-hand sides of a
 // lattice with time extent lt
 inline bool hop_shape_valid(const HopShape& sh, int prec, int nrhs, int lt) {
   if (sh.pair == 1) return prec == PREC_HALF && lt % 2 == 0;
   if (sh.pair == 2) return prec == PREC_HALF;
+  if (sh.pair == 3) return prec == PREC_HALF && nrhs % 2 == 0 && sh.nrb <= nrhs;
   return !(sh.nrb > 1 && sh.nrb > nrhs);  // a block would be mostly idle
+}
+
+// site blocks of one right-hand-side group (the partials each launch writes per right-hand side)
+inline int hop_blocks(const HopShape& sh, int Vh) {
+  const int sites = sh.pair == 1 ? 2 * sh.tx : sh.tx;
+  return (Vh + sites - 1) / sites;
 }
 
 // Returns the number of x-blocks launched (partials per right-hand side), or -1 if the

@@ -16,7 +16,10 @@ __global__ void __launch_bounds__(KT) multi_cdot_kernel(int Vh, VecList vl, Spin
   const int r = blockIdx.y;
   const int i = blockIdx.z;
   const Spinor& v = vl.v[i];
-  double re = 0.0, im = 0.0;
+  // thread and warp sums in the compute precision, block sums in FP64 (FP64 per site is slow here)
+  using T = typename std::conditional<std::is_same<PV, PrecD>::value || std::is_same<PW, PrecD>::value, double,
+                                      float>::type;
+  T re = 0, im = 0;
   for (int idx = blockIdx.x * KT + threadIdx.x; idx < Vh; idx += gridDim.x * KT) {
     cplx<typename PV::real> a[12];
     cplx<typename PW::real> b[12];
@@ -24,16 +27,14 @@ __global__ void __launch_bounds__(KT) multi_cdot_kernel(int Vh, VecList vl, Spin
                     idx, v.stride);
     load_spinor<PW>(b, (const char*)w.v + (size_t)r * w.rhs_bytes, w.norm ? w.norm + (size_t)r * w.norm_rhs_stride : nullptr,
                     idx, w.stride);
-    using T = typename std::conditional<std::is_same<PV, PrecD>::value || std::is_same<PW, PrecD>::value, double,
-                                        float>::type;
     T sr = 0, si = 0;
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
       sr = fmadd((T)a[k].re, (T)b[k].re, fmadd((T)a[k].im, (T)b[k].im, sr));
       si = fmadd((T)a[k].re, (T)b[k].im, fmadd(-(T)a[k].im, (T)b[k].re, si));
     }
-    re += (double)sr;
-    im += (double)si;
+    re += sr;
+    im += si;
   }
   __shared__ double sh[2][KT / 32];
 #pragma unroll
@@ -42,8 +43,8 @@ __global__ void __launch_bounds__(KT) multi_cdot_kernel(int Vh, VecList vl, Spin
     im += __shfl_down_sync(0xffffffffu, im, off);
   }
   if ((threadIdx.x & 31) == 0) {
-    sh[0][threadIdx.x >> 5] = re;
-    sh[1][threadIdx.x >> 5] = im;
+    sh[0][threadIdx.x >> 5] = (double)re;
+    sh[1][threadIdx.x >> 5] = (double)im;
   }
   __syncthreads();
   if (threadIdx.x < 2) {

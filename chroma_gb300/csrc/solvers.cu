@@ -671,6 +671,10 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     int total = 0;
     std::vector<double> prev_rr(n, HUGE_VAL);
     bool rr_exact = false;  // whether the last residual came from the FP64 operator
+    // BiCGStab can break down (rho or (r0, v) -> 0) or stagnate where CG on the normal equations
+    // cannot: once an inner BiCGStab breaks down or its correction is taken back, the remaining
+    // outer steps of this solve run the inner CGNE instead
+    bool bicg_fallback = false;
     for (int it = 0; it <= max_outer; ++it) {
       if (it == 0 && p.zero_guess) {
         blas_copy(g, rd, chi, s);
@@ -703,15 +707,20 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
       // A correction that left the FP64 residual larger than before (an inner solve that broke
       // down) is taken back, and that right-hand side stops with the better iterate.
       bool revert = false;
+      const bool retry_cg = p.solver == GBC_SOLVER_BICGSTAB && !bicg_fallback;
       for (int i = 0; i < n; ++i) {
         const bool back = !done[i] && std::isfinite(prev_rr[i]) && !(rr[i] <= prev_rr[i]);
         c->h_coef[i] = make_double2(back ? -1.0 : 0.0, 0.0);
         c->h_coef[n + i] = make_double2(1.0, 0.0);
         if (back) {
           revert = true;
-          done[i] = 1;
           rr[i] = prev_rr[i];
-          if (status[i] == GBC_OK) status[i] = GBC_ERR_NOT_CONVERGED;
+          if (retry_cg) {
+            bicg_fallback = true;  // this right-hand side goes on with the inner CGNE
+          } else {
+            done[i] = 1;
+            if (status[i] == GBC_OK) status[i] = GBC_ERR_NOT_CONVERGED;
+          }
         }
       }
       if (revert) {
@@ -756,12 +765,17 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
         // flexible GMRES on M~ e = r directly (preconditioned by the learned network if loaded)
         blas_zero(g, es, s);
         st = fgmres(c, pa, sloppy, es, rsl, itol, p.inner_max_iter, p.nkrylov, p.use_precond != 0, active);
-      } else if (p.solver == GBC_SOLVER_BICGSTAB && !mdagm) {
+      } else if (p.solver == GBC_SOLVER_BICGSTAB && !mdagm && !bicg_fallback) {
         // BiCGStab on M~ e = r directly (no normal equations)
         InnerStats bs = bicgstab(c, pa, sloppy, itol, p.inner_max_iter, p.delta, es, rsl, active);
         st.iters = bs.iters;
         st.status = bs.status;
         st.reliable = bs.reliable;
+        for (int i = 0; i < n; ++i)
+          if (active[i] && st.status[i] == GBC_ERR_BREAKDOWN) {
+            bicg_fallback = true;
+            st.status[i] = GBC_OK;  // the correction so far is kept; CGNE takes over
+          }
       } else {
         if (!mdagm) apply_meo(c, pa, true, rsl, rhs, teh, false);
         else blas_copy(g, rhs, rsl, s);

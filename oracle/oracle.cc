@@ -782,6 +782,62 @@ static SolveResult reliable_cg(const Op<double>& A, const Op<float>& AF, const c
 }
 
 // ---------------------------------------------------------------------------------------------
+// InvBiCGStab_a (lib/actions/ferm/invert/invbicgstab.cc:12-200) on M itself, restricted to rb[1]:
+// r = r0 = chi - M psi, p = v = 0, rho_prev = alpha = omega = 1; per iteration
+// rho = <r0|r>, beta = (rho/rho_prev)(alpha/omega), p = r + beta (p - omega v), v = M p,
+// alpha = rho/<r0|v>, s = r - alpha v, t = M s, omega = <t|s>/|t|^2, psi += alpha p + omega s,
+// r = s - omega t; stop when |r|^2 < RsdBiCGStab^2 |chi|^2 (or rho = 0: breakdown, n_count = -1).
+static SolveResult invbicgstab(const Op<double>& M, const cd* chi, cd* psi, double rsd, int maxit) {
+  const Geom& g = *M.g;
+  const long N = g.V * NSP;
+  const auto& odd = g.sites[1];
+  std::vector<cd> r(N), r0(N), p(N), v(N), t(N);
+  SolveResult res{maxit, 0, 0};
+  const double chi_sq = norm2_cb(g, chi, 1);
+  const double rsd_sq = rsd * rsd * chi_sq;
+  eo_op(M, r0.data(), psi, +1);
+  for (long s : odd)
+    for (int k = 0; k < NSP; ++k) {
+      const long i = s * NSP + k;
+      r[i] = r0[i] = chi[i] - r0[i];
+    }
+  cd rho_prev(1.0), alpha(1.0), omega(1.0);
+  double rn = norm2_cb(g, r.data(), 1);
+  for (int k = 1; k <= maxit; ++k) {
+    const cd rho = inner_cb(g, r0.data(), r.data(), 1);
+    if (rho == cd(0.0)) {
+      res.n_count = -1;
+      break;
+    }
+    const cd beta = (rho / rho_prev) * (alpha / omega);
+    for (long s : odd)
+      for (int q = 0; q < NSP; ++q) {
+        const long i = s * NSP + q;
+        p[i] = r[i] + beta * (p[i] - omega * v[i]);
+      }
+    eo_op(M, v.data(), p.data(), +1);
+    alpha = rho / inner_cb(g, r0.data(), v.data(), 1);
+    rho_prev = rho;
+    axpby_cb<double, cd>(g, -alpha, v.data(), cd(1.0), r.data(), 1);  // r now holds s
+    eo_op(M, t.data(), r.data(), +1);
+    omega = inner_cb(g, t.data(), r.data(), 1) / norm2_cb(g, t.data(), 1);
+    for (long s : odd)
+      for (int q = 0; q < NSP; ++q) {
+        const long i = s * NSP + q;
+        psi[i] += omega * r[i] + alpha * p[i];
+        r[i] -= omega * t[i];
+      }
+    rn = norm2_cb(g, r.data(), 1);
+    if (rn < rsd_sq) {
+      res.n_count = k;
+      break;
+    }
+  }
+  res.resid = true_resid_linop(M, chi, psi);
+  res.rel_resid = res.resid / std::sqrt(chi_sq);
+  return res;
+}
+
 // FGMRES (NDefl = 0) following lib/actions/ferm/invert/syssolver_linop_fgmres_dr.{h:31-148,
 // cc:77-195, 256-273, 459-765}.  The preconditioner is a callback on full-lattice arrays.
 // ---------------------------------------------------------------------------------------------
@@ -1128,7 +1184,8 @@ void orc_inner_cb(orc_ctx* c, const double* x, const double* y, int cb, double* 
   out[1] = v.imag();
 }
 
-// solver: 0 = CG (LinOpSysSolverCG), 1 = reliable CG (LinOpSysSolverReliableCGClover), 2 = FGMRES
+// solver: 0 = CG (LinOpSysSolverCG), 1 = reliable CG (LinOpSysSolverReliableCGClover), 2 = FGMRES,
+// 3 = BiCGStab (LinOpSysSolverBiCGStab, syssolver_linop_bicgstab.h:57-75)
 // res[0] = n_count, res[1] = resid, res[2] = rel resid
 int orc_solve(orc_ctx* c, int solver, double* psi, const double* chi, double rsd, int maxit, double delta,
               int nkrylov, precond_fn prec, void* user, double* res) {
@@ -1147,6 +1204,8 @@ int orc_solve(orc_ctx* c, int solver, double* psi, const double* chi, double rsd
     r.rel_resid = r.resid / std::sqrt(norm2_cb(g, b, 1));
   } else if (solver == 2) {
     r = fgmres(*c->op, b, x, rsd, nkrylov, maxit, prec, user);
+  } else if (solver == 3) {
+    r = invbicgstab(*c->op, b, x, rsd, maxit);
   } else {
     return -1;
   }

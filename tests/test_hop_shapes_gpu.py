@@ -3,7 +3,8 @@ the CPU oracle: FP16 storage (5e-3 relative), 1 and 12 right-hand sides, both is
 
 The two-sites-per-thread fp16 kernel pairs cb sites i and i + Vh/2, i.e. (x, y, z, t) with
 (x', y, z, t + Lt/2); lattices with odd Lt/2 (4x6x4x6, 6x4x8x10) give the paired site the other
-x parity and so exercise the index arithmetic of both cases."""
+x parity and so exercise the index arithmetic of both cases.  The two-right-hand-sides-per-thread
+kernel (shapes 12-15) runs only for even nrhs: its pins apply to the 12-RHS cases."""
 import os
 
 import numpy as np
@@ -16,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 KAPPA = 0.115
 CSW = 1.0
-NUM_SHAPES = 12  # the candidates compiled into the library (kHopShapes)
+NUM_SHAPES = 16  # the candidates compiled into the library (kHopShapes)
 
 
 def rel(a, b):
@@ -90,3 +91,31 @@ def test_pair_kernel_mixed_solve(shape):
     r = chi[0] - op.apply(O.OP_MEO, psi[0])
     assert np.sqrt(op.norm2(r) / op.norm2(chi[0])) <= 1.05e-10
     assert rc == 0 and res[0]["status"] == 0
+
+
+@pytest.mark.parametrize("shape", [12, 13, 14, 15])
+def test_rhs_pair_kernel_mixed_solve(shape):
+    """A 12-RHS mixed FP16/FP64 solve whose stencil (and its fused |M psi|^2 reduction) runs on one
+    of the two-right-hand-sides-per-thread shapes: every solution reaches the FP64 true residual
+    1e-10 of the oracle operator."""
+    from oracle import Oracle, OracleOp
+    from oracle import oracle as O
+    dims = (4, 6, 4, 6)
+    o = Oracle()
+    u = o.apply_bc(dims, o.gauge_hot(dims, 0.3, 78), (1, 1, 1, -1))
+    mass = 1 / (2 * KAPPA) - 4
+    op = OracleOp(dims, u, mass, CSW)
+    chi = np.stack([S.z2_noise(dims, 40 + k, cb=1).reshape(-1, 12) for k in range(12)])
+    try:
+        ctx = _context(dims, u, mass, shape)
+        try:
+            psi, res, rc = ctx.solve(chi, solver=G.SOLVER_MIXED, rsd_target=1e-10)
+        finally:
+            ctx.close()
+    finally:
+        os.environ.pop("GBC_SHAPE", None)
+    assert rc == 0
+    for k in range(12):
+        r = chi[k] - op.apply(O.OP_MEO, psi[k])
+        assert np.sqrt(op.norm2(r) / op.norm2(chi[k])) <= 1.05e-10, k
+        assert res[k]["status"] == 0

@@ -267,7 +267,7 @@ def test_symmetric_operator_identities(orc):
     assert np.abs(mm[par == 1] - want[par == 1]).max() < 1e-12 * np.abs(want).max()
 
 
-@pytest.mark.parametrize("solver", [O.SOLVER_CG, O.SOLVER_RELIABLE_CG, O.SOLVER_FGMRES])
+@pytest.mark.parametrize("solver", [O.SOLVER_CG, O.SOLVER_RELIABLE_CG, O.SOLVER_FGMRES, O.SOLVER_BICGSTAB])
 def test_solvers_converge(orc, solver):
     dims = (4, 4, 4, 8)
     u = orc.apply_bc(dims, orc.gauge_hot(dims, 0.3, 51))
@@ -279,6 +279,19 @@ def test_solvers_converge(orc, solver):
     true_rel = np.sqrt(op.norm2(r) / op.norm2(chi))
     assert abs(true_rel - res["rel_resid"]) < 1e-3 * true_rel + 1e-16
     assert true_rel < 5e-9
+
+
+def test_bicgstab_matches_cg(orc):
+    # BiCGStab on M~ (no normal equations) and CGNE reach the same solution, BiCGStab in fewer
+    # operator applications (2 per iteration for both)
+    dims = (4, 4, 4, 8)
+    u = orc.apply_bc(dims, orc.gauge_hot(dims, 0.3, 52))
+    op = OracleOp(dims, u, 1 / (2 * 0.12) - 4, 1.2)
+    chi = rand_spinor(dims, 9, cb=1)
+    x_cg, r_cg = op.solve(chi, solver=O.SOLVER_CG, rsd=1e-12, maxit=5000)
+    x_bi, r_bi = op.solve(chi, solver=O.SOLVER_BICGSTAB, rsd=1e-12, maxit=5000)
+    assert 0 < r_bi["n_count"] < r_cg["n_count"], (r_bi, r_cg)
+    assert np.linalg.norm(x_bi - x_cg) < 1e-9 * np.linalg.norm(x_cg)
 
 
 def test_qprop_full_residual(orc):
