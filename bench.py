@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--dims", default=None, help="override lattice, e.g. 16,16,16,32 (testing only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1)
-    ap.add_argument("--op-only", default=None, choices=["dslash16", "dslash32", "dslash64", "meo16"],
+    ap.add_argument("--op-only", default=None, choices=["dslash16", "dslash32", "dslash64", "meo16", "meo64"],
                     help="profiling mode: set up the workload and time one operator only")
     ap.add_argument("--nrhs", type=int, default=12)
     ap.add_argument("--recon", type=int, default=12, choices=[12, 18])
@@ -69,7 +69,8 @@ def op_only(args):
                     sloppy_reconstruct=args.recon)
     ctx.load_gauge(links)
     op, prec = {"dslash16": (G.OP_DSLASH, G.PREC_HALF), "dslash32": (G.OP_DSLASH, G.PREC_SINGLE),
-                "dslash64": (G.OP_DSLASH, G.PREC_DOUBLE), "meo16": (G.OP_MEO, G.PREC_HALF)}[args.op_only]
+                "dslash64": (G.OP_DSLASH, G.PREC_DOUBLE), "meo16": (G.OP_MEO, G.PREC_HALF),
+                "meo64": (G.OP_MEO, G.PREC_DOUBLE)}[args.op_only]
     sec, byts = ctx.time_operator(op, prec, nrhs=args.nrhs, iters=args.iters, flush_l2=True)
     print(json.dumps({"op": args.op_only, "dims": dims, "nrhs": args.nrhs, "seconds": sec, "bytes": byts,
                       "GBps": byts / sec / 1e9, "tuned": ctx.tune_report().strip().splitlines()}), flush=True)

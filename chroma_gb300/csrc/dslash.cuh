@@ -351,9 +351,10 @@ __device__ __forceinline__ void hop_dir_f2(float2 (&acc)[12], const HopArgs& a, 
 // Each (site, direction) link is loaded and reconstructed once per block and kept in shared memory
 // as the pairs (ur, ur, -ui, ui) that the packed complex multiply consumes; without this every
 // right-hand side would redo the 12-real reconstruction.  Layout [dir][element][site] keeps a
-// warp's 32 sites on consecutive 16-byte words.
+// warp's 32 sites on consecutive 16-byte words.  The neighbour index of each hop goes to nsm
+// [dir][site], so the threads of the block's right-hand sides need no coordinate arithmetic.
 template <typename P, int RECON, int TX>
-__device__ __forceinline__ void stage_links(float4 (*lsm)[9][TX], const HopArgs& a, int sblock) {
+__device__ __forceinline__ void stage_links(float4 (*lsm)[9][TX], int (*nsm)[TX], const HopArgs& a, int sblock) {
   const Geom& g = a.g;
   for (int p = threadIdx.x; p < 8 * TX; p += blockDim.x) {
     const int s = p % TX, d = p / TX;
@@ -366,11 +367,16 @@ __device__ __forceinline__ void stage_links(float4 (*lsm)[9][TX], const HopArgs&
     if (!bwd) {
       const float sign = (mu == 3 && c.x[3] == g.L[3] - 1) ? (float)g.t_sign : 1.0f;
       load_link<P, RECON>(u, a.gauge_fwd[mu], idx, g.stride, sign);
+      Coord n = c;
+      n.x[mu] = c.x[mu] + 1 == g.L[mu] ? 0 : c.x[mu] + 1;
+      nsm[d][s] = cb_index(g, n);
     } else {
       Coord n = c;
       n.x[mu] = c.x[mu] == 0 ? g.L[mu] - 1 : c.x[mu] - 1;
       const float sign = (mu == 3 && n.x[3] == g.L[3] - 1) ? (float)g.t_sign : 1.0f;
-      load_link<P, RECON>(u, a.gauge_bwd[mu], cb_index(g, n), g.stride, sign);
+      const int j = cb_index(g, n);
+      load_link<P, RECON>(u, a.gauge_bwd[mu], j, g.stride, sign);
+      nsm[d][s] = j;
     }
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -406,25 +412,21 @@ __device__ __forceinline__ void matvec_sm(float2 (&uh)[2][3], const float4 (*lsm
 }
 
 template <typename P, int MU, bool DAG, int TX>
-__device__ __forceinline__ void hop_dir_sm(float2 (&acc)[12], const float4 (*lsm)[9][TX], int s, const HopArgs& a,
-                                           const Coord& c, const char* in, const float* in_norm) {
+__device__ __forceinline__ void hop_dir_sm(float2 (&acc)[12], const float4 (*lsm)[9][TX], const int (*nsm)[TX], int s,
+                                           const HopArgs& a, const char* in, const float* in_norm) {
   constexpr int SF = DAG ? +1 : -1;
   constexpr int SB = DAG ? -1 : +1;
   const Geom& g = a.g;
   float2 h[2][3], uh[2][3];
   float n;
   {
-    Coord nb = c;
-    nb.x[MU] = c.x[MU] + 1 == g.L[MU] ? 0 : c.x[MU] + 1;
-    load_project<P, MU, SF>(h, n, in, in_norm, cb_index(g, nb), g.stride);
+    load_project<P, MU, SF>(h, n, in, in_norm, nsm[2 * MU][s], g.stride);
     scale_f2<P>(h, n);
     matvec_sm<TX>(uh, lsm, 2 * MU, s, h);
     reconstruct_f2<MU, SF>(acc, uh);
   }
   {
-    Coord nb = c;
-    nb.x[MU] = c.x[MU] == 0 ? g.L[MU] - 1 : c.x[MU] - 1;
-    load_project<P, MU, SB>(h, n, in, in_norm, cb_index(g, nb), g.stride);
+    load_project<P, MU, SB>(h, n, in, in_norm, nsm[2 * MU + 1][s], g.stride);
     scale_f2<P>(h, n);
     matvec_sm<TX>(uh, lsm, 2 * MU + 1, s, h);
     reconstruct_f2<MU, SB>(acc, uh);
@@ -529,8 +531,9 @@ __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group
   // 8 x 9 x 32 x 16 B = 36 KiB of static shared memory for 32-site blocks
   constexpr bool kShared = NRB > 1 && TX == 32 && std::is_same<T, float>::value;
   __shared__ float4 lsm[kShared ? 8 : 1][9][kShared ? TX : 1];
+  __shared__ int nsm[kShared ? 8 : 1][kShared ? TX : 1];
   if constexpr (kShared) {
-    stage_links<P, RECON, TX>(lsm, a, sblock);
+    stage_links<P, RECON, TX>(lsm, nsm, a, sblock);
     __syncthreads();
   }
   // |out|^2: thread and warp sums in the compute precision, block sums in FP64
@@ -546,10 +549,10 @@ __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group
       for (int k = 0; k < 12; ++k) accf[k] = make_float2(0.f, 0.f);
       if constexpr (kShared) {
         const int s = tid % TX;
-        hop_dir_sm<P, 0, DAG, TX>(accf, lsm, s, a, c, in, in_norm);
-        hop_dir_sm<P, 1, DAG, TX>(accf, lsm, s, a, c, in, in_norm);
-        hop_dir_sm<P, 2, DAG, TX>(accf, lsm, s, a, c, in, in_norm);
-        hop_dir_sm<P, 3, DAG, TX>(accf, lsm, s, a, c, in, in_norm);
+        hop_dir_sm<P, 0, DAG, TX>(accf, lsm, nsm, s, a, in, in_norm);
+        hop_dir_sm<P, 1, DAG, TX>(accf, lsm, nsm, s, a, in, in_norm);
+        hop_dir_sm<P, 2, DAG, TX>(accf, lsm, nsm, s, a, in, in_norm);
+        hop_dir_sm<P, 3, DAG, TX>(accf, lsm, nsm, s, a, in, in_norm);
       } else {
         hop_dir_f2<P, RECON, 0, DAG>(accf, a, c, idx, in, in_norm);
         hop_dir_f2<P, RECON, 1, DAG>(accf, a, c, idx, in, in_norm);

@@ -7,9 +7,9 @@
 // form of the two-sites-per-thread kernel): the link, identical for both lanes, is read once per
 // thread from shared memory as (ur, ur, ui, ui) and feeds both right-hand sides; the factors +-i
 // of the projectors only relabel real and imaginary parts; the two neighbour norms fold into the
-// accumulation FMAs.  The 8 neighbour indices are computed once per thread for both right-hand
-// sides.  Lanes 2k and 2k + 1 of a warp work on the same site (two pairs of right-hand sides), so
-// each 16-byte link word read from shared memory serves two lanes.
+// accumulation FMAs.  The 8 neighbour indices are staged in shared memory with the links, once
+// per block.  Lanes 2k and 2k + 1 of a warp work on the same site (two pairs of right-hand sides),
+// so each 16-byte link word read from shared memory serves two lanes.
 //
 // Block: TS sites x NRB right-hand sides, TS * NRB / 2 threads; nrhs must be even.
 #pragma once
@@ -19,9 +19,10 @@
 namespace gbc {
 
 // the 8 links of a block's TS sites, reconstructed once, as (ur, ur, ui, ui); backward hops hold
-// U^dag of the neighbour's link.  Layout [hop][element][site].
+// U^dag of the neighbour's link.  Layout [hop][element][site]; the neighbour index of each hop in
+// nsm[hop][site].
 template <int RECON, int TS>
-__device__ __forceinline__ void stage_links_rp(float4 (*lsm)[9][TS], const HopArgs& a, int sblock) {
+__device__ __forceinline__ void stage_links_rp(float4 (*lsm)[9][TS], int (*nsm)[TS], const HopArgs& a, int sblock) {
   const Geom& g = a.g;
   for (int p = threadIdx.x; p < 8 * TS; p += blockDim.x) {
     const int s = p % TS, d = p / TS;
@@ -34,11 +35,16 @@ __device__ __forceinline__ void stage_links_rp(float4 (*lsm)[9][TS], const HopAr
     if (!bwd) {
       const float sign = (mu == 3 && c.x[3] == g.L[3] - 1) ? (float)g.t_sign : 1.0f;
       load_link<PrecH, RECON>(u, a.gauge_fwd[mu], idx, g.stride, sign);
+      Coord n = c;
+      n.x[mu] = c.x[mu] + 1 == g.L[mu] ? 0 : c.x[mu] + 1;
+      nsm[d][s] = cb_index(g, n);
     } else {
       Coord n = c;
       n.x[mu] = c.x[mu] == 0 ? g.L[mu] - 1 : c.x[mu] - 1;
       const float sign = (mu == 3 && n.x[3] == g.L[3] - 1) ? (float)g.t_sign : 1.0f;
-      load_link<PrecH, RECON>(u, a.gauge_bwd[mu], cb_index(g, n), g.stride, sign);
+      const int j = cb_index(g, n);
+      load_link<PrecH, RECON>(u, a.gauge_bwd[mu], j, g.stride, sign);
+      nsm[d][s] = j;
     }
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -110,20 +116,20 @@ __device__ __forceinline__ void mult_rebuild_rp(C2 (&acc)[12], const float4 (*lk
 }
 
 template <int MU, bool DAG, int TS>
-__device__ __forceinline__ void hop_dir_rp(C2 (&acc)[12], const float4 (*lsm)[9][TS], int s, const HopSites& hs,
+__device__ __forceinline__ void hop_dir_rp(C2 (&acc)[12], const float4 (*lsm)[9][TS], const int (*nsm)[TS], int s,
                                            const char* in0, const char* in1, const float* nm0, const float* nm1,
                                            int stride) {
   constexpr int SF = DAG ? +1 : -1;  // forward:  (1 - isign gamma)
   constexpr int SB = DAG ? -1 : +1;  // backward: (1 + isign gamma)
   C2 h[2][3];
   {
-    const int j = hs.j[2 * MU];
+    const int j = nsm[2 * MU][s];
     load_project_rp<MU, SF>(h, in0, in1, j, stride);
     const float2 n = make_float2(ldg(nm0 + j), ldg(nm1 + j));
     mult_rebuild_rp<MU, SF, TS>(acc, lsm[2 * MU], s, h, n);
   }
   {
-    const int j = hs.j[2 * MU + 1];
+    const int j = nsm[2 * MU + 1][s];
     load_project_rp<MU, SB>(h, in0, in1, j, stride);
     const float2 n = make_float2(ldg(nm0 + j), ldg(nm1 + j));
     mult_rebuild_rp<MU, SB, TS>(acc, lsm[2 * MU + 1], s, h, n);
@@ -147,11 +153,11 @@ __global__ void __launch_bounds__(TS * NRB / 2, MINB) hop_kernel_rp(const HopArg
   const int idx = sblock * TS + s;
   const Geom& g = a.g;
   __shared__ float4 lsm[8][9][TS];
-  stage_links_rp<RECON, TS>(lsm, a, sblock);
+  __shared__ int nsm[8][TS];
+  stage_links_rp<RECON, TS>(lsm, nsm, a, sblock);
   __syncthreads();
   float l0 = 0.f, l1 = 0.f;  // thread and warp sums in FP32, block sums in FP64
   if (idx < g.Vh && r0 < a.nrhs) {
-    const HopSites hs = hop_sites(g, cb_coords(g, idx, a.out_parity));
     const char* in0 = (const char*)a.in + (size_t)r0 * a.in_rhs_bytes;
     const char* in1 = in0 + a.in_rhs_bytes;
     const float* nm0 = a.in_norm + (size_t)r0 * a.norm_rhs_stride;
@@ -159,10 +165,10 @@ __global__ void __launch_bounds__(TS * NRB / 2, MINB) hop_kernel_rp(const HopArg
     C2 acc[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) acc[k] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-    hop_dir_rp<0, DAG, TS>(acc, lsm, s, hs, in0, in1, nm0, nm1, g.stride);
-    hop_dir_rp<1, DAG, TS>(acc, lsm, s, hs, in0, in1, nm0, nm1, g.stride);
-    hop_dir_rp<2, DAG, TS>(acc, lsm, s, hs, in0, in1, nm0, nm1, g.stride);
-    hop_dir_rp<3, DAG, TS>(acc, lsm, s, hs, in0, in1, nm0, nm1, g.stride);
+    hop_dir_rp<0, DAG, TS>(acc, lsm, nsm, s, in0, in1, nm0, nm1, g.stride);
+    hop_dir_rp<1, DAG, TS>(acc, lsm, nsm, s, in0, in1, nm0, nm1, g.stride);
+    hop_dir_rp<2, DAG, TS>(acc, lsm, nsm, s, in0, in1, nm0, nm1, g.stride);
+    hop_dir_rp<3, DAG, TS>(acc, lsm, nsm, s, in0, in1, nm0, nm1, g.stride);
     cplx<float> sa[12], sb[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
