@@ -148,11 +148,12 @@ def test_solvers_reach_1e10(setup, solver, sloppy):
         assert o10["n_count"] <= res[0]["n_count"] <= o10["n_count"] + 20, (o10, res)
 
 
-def test_full_system_qprop(setup):
+@pytest.mark.parametrize("solver", [G.SOLVER_MIXED, G.SOLVER_BICGSTAB], ids=["cgne", "bicgstab"])
+def test_full_system_qprop(setup, solver):
     dims, op, ctx = setup
     from oracle import oracle as O
     chi = S.gaussian(dims, 21).reshape(1, -1, 12)
-    psi, res, rc = ctx.solve(chi, solver=G.SOLVER_MIXED, system=G.SYS_FULL, rsd_target=1e-10)
+    psi, res, rc = ctx.solve(chi, solver=solver, system=G.SYS_FULL, rsd_target=1e-10)
     assert rc == 0
     r = op.apply(O.OP_UNPREC, psi[0]) - chi[0]
     full_rel = np.linalg.norm(r) / np.linalg.norm(chi[0])
@@ -170,9 +171,11 @@ def test_mdagm_system(setup):
     assert np.sqrt(op.norm2(r) / op.norm2(chi[0])) <= 1.05e-10
 
 
-def test_point_sources_near_critical_16x32():
+@pytest.mark.parametrize("solver,delta", [(G.SOLVER_MIXED, 0.1), (G.SOLVER_BICGSTAB, 0.01)], ids=["cgne", "bicgstab"])
+def test_point_sources_near_critical_16x32(solver, delta):
     """The propagator workload's parameters (kappa 0.1250, c_sw 1.6) on 16^3 x 32: the 12 point
-    sources as one batch through the full system, each to FP64 true residual 1e-10."""
+    sources as one batch through the full system, each to FP64 true residual 1e-10 (inner CGNE, and
+    the inner BiCGStab with the headline's Delta)."""
     from oracle import Oracle, OracleOp
     from oracle import oracle as O
     dims = (16, 16, 16, 32)
@@ -184,7 +187,7 @@ def test_point_sources_near_critical_16x32():
     try:
         ctx.load_gauge(u)
         src = S.point_sources(dims).reshape(12, -1, 12)
-        psi, res, rc = ctx.solve(src, solver=G.SOLVER_MIXED, system=G.SYS_FULL, rsd_target=1e-10)
+        psi, res, rc = ctx.solve(src, solver=solver, system=G.SYS_FULL, rsd_target=1e-10, delta=delta)
         assert rc == 0, res
         for k in (0, 7, 11):
             r = op.apply(O.OP_UNPREC, psi[k]) - src[k]

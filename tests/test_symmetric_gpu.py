@@ -50,8 +50,9 @@ def test_symmetric_operator_matches_oracle(setup, prec):
 
 @pytest.mark.parametrize("solver,sloppy,system", [(G.SOLVER_CG, 0, G.SYS_SYM), (G.SOLVER_MIXED, G.PREC_HALF, G.SYS_SYM),
                                                   (G.SOLVER_FGMRES, G.PREC_SINGLE, G.SYS_SYM),
-                                                  (G.SOLVER_MIXED, G.PREC_HALF, G.SYS_SYM_MDAGM)],
-                         ids=["cg64", "mixed16", "fgmres32", "mdagm-mixed16"])
+                                                  (G.SOLVER_MIXED, G.PREC_HALF, G.SYS_SYM_MDAGM),
+                                                  (G.SOLVER_BICGSTAB, G.PREC_HALF, G.SYS_SYM)],
+                         ids=["cg64", "mixed16", "fgmres32", "mdagm-mixed16", "bicgstab16"])
 def test_symmetric_solves(setup, solver, sloppy, system):
     from oracle import oracle as O
     dims, op, ctx = setup

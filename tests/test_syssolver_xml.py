@@ -86,3 +86,15 @@ def test_unknown_solver_type():
 def test_kappa_to_mass():
     assert SS.kappa_to_mass(0.125) == 0.0
     assert np.isclose(SS.kappa_to_mass(0.115), 1 / 0.23 - 4)
+
+
+@pytest.mark.parametrize("name,code", [("CG", "SOLVER_CG"), ("RELIABLE_CG", "SOLVER_RELIABLE_CG"),
+                                       ("MIXED", "SOLVER_MIXED"), ("BICGSTAB", "SOLVER_BICGSTAB"),
+                                       ("GCR", "SOLVER_FGMRES"), ("FGMRES", "SOLVER_FGMRES")])
+def test_solver_type_map(name, code):
+    """QUDA's SolverType strings select the library solver: BICGSTAB the inner reliable BiCGStab,
+    GCR the flexible-Krylov FGMRES (both minimise over a flexible space)."""
+    from chroma_gb300 import gbclover as G
+    p = SS.SysSolverGB300CloverParams.from_xml(QUDA_XML.replace("<SolverType>CG", f"<SolverType>{name}", 1))
+    assert p.SolverType == name
+    assert SS._SOLVER[name] == getattr(G, code)
