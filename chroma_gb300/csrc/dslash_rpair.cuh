@@ -136,6 +136,35 @@ __device__ __forceinline__ void hop_dir_rp(C2 (&acc)[12], const float4 (*lsm)[9]
   }
 }
 
+// |out|^2 partials of a two-RHS block: lanes of one parity share a pair group, so a butterfly over
+// the even lane offsets leaves the even-lane sums in lane 0 and the odd-lane sums in lane 1; then a
+// fixed-order sum over the TS/16 warps of each pair group (bitwise repeatable)
+template <int TS, int NRB>
+__device__ __forceinline__ void rp_block_sums(const HopArgs& a, float l0, float l1, int group, int sblock) {
+  constexpr int SW = TS / 16;
+  const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
+  __shared__ double wsum[TS * NRB / 64][2][2];
+#pragma unroll
+  for (int off = 16; off >= 2; off >>= 1) {
+    l0 += __shfl_xor_sync(0xffffffffu, l0, off);
+    l1 += __shfl_xor_sync(0xffffffffu, l1, off);
+  }
+  if (l < 2) {
+    wsum[w][l][0] = (double)l0;
+    wsum[w][l][1] = (double)l1;
+  }
+  __syncthreads();
+  if (tid < NRB) {
+    const int q = tid >> 1;
+    const int r = group * NRB + tid;
+    double sum = 0.0;
+#pragma unroll
+    for (int k = 0; k < SW; ++k) sum += wsum[(q >> 1) * SW + k][q & 1][tid & 1];
+    if (r < a.nrhs) a.partials[(size_t)r * a.part_stride + sblock] = sum;
+  }
+}
+
+
 // Grid: ceil(Vh / TS) site blocks x ceil(nrhs / NRB) right-hand-side groups, groups fastest.
 // Thread t: warp w = t / 32, lane l; site (w % (TS/16)) * 16 + l / 2 of the block, pair group
 // (w / (TS/16)) * 2 + (l & 1), i.e. right-hand sides 2 pg and 2 pg + 1 of the group.
@@ -178,30 +207,7 @@ __global__ void __launch_bounds__(TS * NRB / 2, MINB) hop_kernel_rp(const HopArg
     l0 = hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, r0, idx, sa);
     l1 = hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, r0 + 1, idx, sb);
   }
-  if constexpr (REDUCE) {
-    // lanes of one parity share a pair group: butterfly over the even lane offsets leaves the
-    // even-lane sums in lane 0 and the odd-lane sums in lane 1; then a fixed-order sum over the
-    // TS/16 warps of each pair group (bitwise repeatable)
-    __shared__ double wsum[TS * NRB / 64][2][2];
-#pragma unroll
-    for (int off = 16; off >= 2; off >>= 1) {
-      l0 += __shfl_xor_sync(0xffffffffu, l0, off);
-      l1 += __shfl_xor_sync(0xffffffffu, l1, off);
-    }
-    if (l < 2) {
-      wsum[w][l][0] = (double)l0;
-      wsum[w][l][1] = (double)l1;
-    }
-    __syncthreads();
-    if (tid < NRB) {
-      const int q = tid >> 1;
-      const int r = group * NRB + tid;
-      double sum = 0.0;
-#pragma unroll
-      for (int k = 0; k < SW; ++k) sum += wsum[(q >> 1) * SW + k][q & 1][tid & 1];
-      if (r < a.nrhs) a.partials[(size_t)r * a.part_stride + sblock] = sum;
-    }
-  }
+  if constexpr (REDUCE) rp_block_sums<TS, NRB>(a, l0, l1, group, sblock);
 }
 
 }  // namespace gbc

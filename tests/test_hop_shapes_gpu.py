@@ -4,7 +4,7 @@ the CPU oracle: FP16 storage (5e-3 relative), 1 and 12 right-hand sides, both is
 The two-sites-per-thread fp16 kernel pairs cb sites i and i + Vh/2, i.e. (x, y, z, t) with
 (x', y, z, t + Lt/2); lattices with odd Lt/2 (4x6x4x6, 6x4x8x10) give the paired site the other
 x parity and so exercise the index arithmetic of both cases.  The two-right-hand-sides-per-thread
-kernel (shapes 12-15) runs only for even nrhs: its pins apply to the 12-RHS cases."""
+kernels (shapes 12-15) run only for even nrhs: their pins apply to the 12-RHS cases."""
 import os
 
 import numpy as np
