@@ -104,10 +104,14 @@ __device__ __forceinline__ float site_norm(const Spinor& f, int idx, int r) {
 
 // grid-stride site loop, one y-block row per right-hand side, NRED sums per right-hand side
 // F::kMinb resident blocks per SM: 4 (64 registers) for the FP32 accumulators, 2 for FP64
+// A right-hand side that has converged (sc[r].active == 0) is skipped: its vectors are frozen and
+// its partial rows are never read.
 template <int NRED, class F>
-__global__ void __launch_bounds__(BT, F::kMinb) bi_site_kernel(int Vh, F f, double* partials, int part_stride, int nrhs) {
+__global__ void __launch_bounds__(BT, F::kMinb) bi_site_kernel(int Vh, F f, const BiScal* sc, double* partials,
+                                                               int part_stride, int nrhs) {
   using A = typename AccOf<F>::type;  // thread and warp sums in the compute precision
   const int r = blockIdx.y;
+  if (!sc[r].active) return;  // uniform over the block
   A acc[NRED > 0 ? NRED : 1];
 #pragma unroll
   for (int q = 0; q < (NRED > 0 ? NRED : 1); ++q) acc[q] = 0;
@@ -298,11 +302,11 @@ __global__ void bi_beta(BiScal* sc, const double* res, int n) {
 }
 
 template <int NRED, class F>
-void run(gbc_ctx* c, int nrhs, const F& f) {
+void run(gbc_ctx* c, int nrhs, const BiScal* sc, const F& f) {
   const Geom& g = c->g;
   dim3 grid(blas_blocks(g), nrhs);
   const Red rd = red(c);
-  bi_site_kernel<NRED, F><<<grid, BT, 0, c->stream>>>(g.Vh, f, rd.partials, rd.part_stride, nrhs);
+  bi_site_kernel<NRED, F><<<grid, BT, 0, c->stream>>>(g.Vh, f, sc, rd.partials, rd.part_stride, nrhs);
   count_launch();
   if (NRED > 0) reduce_finalize(rd, NRED, nrhs, grid.x, c->stream);
 }
@@ -312,19 +316,24 @@ void iteration(gbc_ctx* c, int po, BiScal* sc, int n, const Spinor& x, const Spi
                const Spinor& p, const Spinor& v, const Spinor& s, const Spinor& t, const Spinor& te) {
   cudaStream_t st = c->stream;
   const int nth = ((n + 31) / 32) * 32;  // one thread per right-hand side
-  apply_meo(c, po, false, p, v, te, false);
+  apply_meo(c, po, false, p, v, te, RED_NONE);
   blas_cdot(c->g, r0, v, red(c), st);
   bi_alpha<<<1, nth, 0, st>>>(sc, c->d_result, n);
   count_launch();
-  run<0>(c, n, SUpdF<PA, PO>{sc, r, v, s});
-  apply_meo(c, po, false, s, t, te, false);
-  run<3>(c, n, TsTtF<PO>{t, s});
+  run<0>(c, n, sc, SUpdF<PA, PO>{sc, r, v, s});
+  if (c->sym) {
+    apply_meo(c, po, false, s, t, te, RED_NONE);
+    run<3>(c, n, sc, TsTtF<PO>{t, s});
+  } else {
+    // (t, s) and (t, t) summed in the epilogue of the stencil launch that writes t (s is its self)
+    apply_meo(c, po, false, s, t, te, RED_DOT_SELF);
+  }
   bi_omega<<<1, nth, 0, st>>>(sc, c->d_result, n);
   count_launch();
-  run<3>(c, n, XRUpdF<PA, PO>{sc, x, r, p, v, t, r0});
+  run<3>(c, n, sc, XRUpdF<PA, PO>{sc, x, r, p, v, t, r0});
   bi_beta<<<1, nth, 0, st>>>(sc, c->d_result, n);
   count_launch();
-  run<0>(c, n, PUpdF<PA, PO>{sc, r, p, v});
+  run<0>(c, n, sc, PUpdF<PA, PO>{sc, r, p, v});
 }
 
 }  // namespace
@@ -387,6 +396,18 @@ InnerStats bicgstab(gbc_ctx* c, int pa, int po, double tol, int maxit, double de
   }
   {
     GBC_CUDA(cudaMemcpyAsync(d_sc, hs.data(), sizeof(BiScal) * n, cudaMemcpyHostToDevice, st));
+    // the stencil launches of this solve skip right-hand sides whose device flag says converged;
+    // the flags are unset again however the solve ends
+    static_assert(sizeof(BiScal) % sizeof(int) == 0, "flag stride in ints");
+    struct ActiveScope {
+      gbc_ctx* c;
+      ~ActiveScope() {
+        c->hop_active = nullptr;
+        c->hop_active_stride = 0;
+      }
+    } active_scope{c};
+    c->hop_active = &d_sc[0].active;
+    c->hop_active_stride = (int)(sizeof(BiScal) / sizeof(int));
     auto body = [&]() {
       if (pa == PREC_DOUBLE) iteration<PrecD, PrecD>(c, po, d_sc, n, x, r, r0, p, v, s, t, te);
       else if (po == PREC_SINGLE) iteration<PrecS, PrecS>(c, po, d_sc, n, x, r, r0, p, v, s, t, te);

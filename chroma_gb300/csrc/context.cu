@@ -167,10 +167,10 @@ static int default_shape(int nrhs) {
   return 1;
 }
 
-int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce, const HopArgs& h) {
+int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, int reduce, const HopArgs& h) {
   // (precision, epilogue, isign, reduction) in the high bits, nrhs (any size) in the low 32
   const long long key =
-      ((((long long)pidx(prec) * 4 + mode) * 2 + (dag ? 1 : 0)) * 2 + (reduce ? 1 : 0)) << 32 | (unsigned)h.nrhs;
+      ((((long long)pidx(prec) * 4 + mode) * 2 + (dag ? 1 : 0)) * 3 + reduce) << 32 | (unsigned)h.nrhs;
   auto it = c->tuned.find(key);
   if (it != c->tuned.end()) return it->second;
   int best = default_shape(h.nrhs);
@@ -211,7 +211,7 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce
     cudaEventDestroy(e1);
     char line[160];
     snprintf(line, sizeof line, "prec=%d mode=%d dag=%d reduce=%d nrhs=%d -> tx=%d nrb=%d minb=%d pair=%d (%.1f us)\n",
-             prec, mode, dag ? 1 : 0, reduce ? 1 : 0, h.nrhs, kHopShapes[best].tx, kHopShapes[best].nrb,
+             prec, mode, dag ? 1 : 0, reduce, h.nrhs, kHopShapes[best].tx, kHopShapes[best].nrb,
              kHopShapes[best].minb, kHopShapes[best].pair, best_ms / 3 * 1e3);
     c->tune_log += line;
   }
@@ -220,7 +220,7 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, bool reduce
 }
 
 void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, const Spinor& in, const Spinor& out,
-         const Spinor* self, const void* clov, bool reduce, double twist) {
+         const Spinor* self, const void* clov, int reduce, double twist) {
   const PrecFields& f = c->pf[pidx(prec)];
   HopArgs h{};
   h.g = c->g;
@@ -247,16 +247,18 @@ void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, con
   h.twist = twist;
   h.partials = c->d_partials;
   h.part_stride = c->part_stride;
+  h.active = c->hop_active;
+  h.active_stride = c->hop_active_stride;
   const HopShape sh = kHopShapes[tuned_shape(c, prec, f.recon, mode, dag, reduce, h)];
   if (hop_blocks(sh, h.g.Vh) > c->part_stride) throw std::string("partials buffer too small");
   int nb = hop_launch(prec, f.recon, mode, dag, reduce, h, sh, c->stream);
   if (nb < 0) throw std::string("hopping kernel variant not compiled");
   count_launch();
   GBC_CUDA(cudaGetLastError());
-  if (reduce) reduce_finalize(red(c), 1, in.nrhs, nb, c->stream);
+  if (reduce) reduce_finalize(red(c), reduce == RED_DOT_SELF ? 3 : 1, in.nrhs, nb, c->stream);
 }
 
-void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, bool reduce) {
+void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, int reduce) {
   if (c->sym) return apply_seo(c, prec, dag, in, out, tmp_e, reduce);
   const PrecFields& f = c->pf[pidx(prec)];
   // t_e = A_ee^-1 D_eo in_o ;  out_o = A_oo in_o - 1/4 D_oe t_e  (+ isign i mu gamma_5 in_o)
@@ -286,7 +288,7 @@ void ensure_sym(gbc_ctx* c, int prec) {
 //   MINUS  out = in - 1/4 D_oe^dag A_ee^-1 D_eo^dag A_oo^-1 in
 // The last step leaves 1/4 (...) in out and blas_xmy_norm2 turns it into in - out with |out|^2.
 void apply_seo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e,
-               bool reduce) {
+               int reduce) {
   ensure_sym(c, prec);
   const PrecFields& f = c->pf[pidx(prec)];
   if (!dag) {

@@ -100,6 +100,10 @@ struct gbc_ctx {
   // device scalars of the inner BiCGStab (bicgstab.cu), bisc_cap right-hand sides
   void* d_bisc = nullptr;
   int bisc_cap = 0;
+  // per-right-hand-side device flags the stencil launches honour while set (HopArgs::active): the
+  // inner BiCGStab points them at its scalars so that converged right-hand sides cost nothing
+  const int* hop_active = nullptr;
+  int hop_active_stride = 0;
 };
 
 namespace gbc {
@@ -115,12 +119,12 @@ Red red(gbc_ctx* c);
 // ---- operator blocks on device fields (all of precision prec) ------------------------------
 // out(out_parity) = mode-epilogue of a * D'(in)
 void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, const Spinor& in, const Spinor& out,
-         const Spinor* self, const void* clov, bool reduce, double twist = 0.0);
+         const Spinor* self, const void* clov, int reduce, double twist = 0.0);
 // out_o = M~ in_o (dag: M~^dag); reduce => |out|^2 in red(c).result[0][rhs]
-void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, bool reduce);
+void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, int reduce);
 void apply_clover(gbc_ctx* c, int prec, int parity, bool inverse, const Spinor& in, const Spinor& out);
 // out_o = M_s in_o (dag: M_s^dag), the symmetric operator; reduce => |out|^2 as apply_meo
-void apply_seo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, bool reduce);
+void apply_seo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, int reduce);
 void ensure_sym(gbc_ctx* c, int prec);  // pack A_oo^-1 in this precision
 // routes apply_meo to the symmetric operator while it lives
 struct SymScope {

@@ -436,18 +436,37 @@ __device__ __forceinline__ void hop_dir_sm(float2 (&acc)[12], const float4 (*lsm
 // Grid: one dimension, right-hand-side groups fastest (block b covers sites (b / ng) * TX ... and
 // right-hand sides (b % ng) * NRB ...), so the groups that share a site range run together and
 // their link reads after the first come from L2.  MINB caps the registers (MINB resident blocks).
-template <typename P, int RECON, int MODE, bool DAG, bool REDUCE, int TX, int NRB>
+template <typename P, int RECON, int MODE, bool DAG, int REDUCE, int TX, int NRB>
 __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group);
 
+// site sums of a fused reduction (RED_NORM: q[0] = |out|^2; RED_DOT_SELF: q = Re, Im (out, self),
+// |out|^2), in the compute precision
+template <typename T>
+struct Sums3 {
+  T q[3];
+};
+template <int RED>
+__host__ __device__ constexpr int red_count() {
+  return RED == RED_DOT_SELF ? 3 : RED == RED_NORM ? 1 : 0;
+}
+template <typename T>
+__device__ __forceinline__ Sums3<T> operator+(Sums3<T> a, const Sums3<T>& b) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q) a.q[q] += b.q[q];
+  return a;
+}
+
 // The MODE epilogue of one output site: out = a D' psi, T (a D' psi) or T self + a D' psi
-// (+ twist), stored in the output precision; returns |out|^2 of the site when REDUCE.
-template <typename P, int MODE, bool DAG, bool REDUCE>
-__device__ __forceinline__ typename P::real hop_epilogue(const HopArgs& a, int rhs, int idx,
-                                                         const cplx<typename P::real> (&acc)[12]) {
+// (+ twist), stored in the output precision; returns the site sums of the REDUCE kind.
+template <typename P, int MODE, bool DAG, int REDUCE>
+__device__ __forceinline__ Sums3<typename P::real> hop_epilogue(const HopArgs& a, int rhs, int idx,
+                                                                const cplx<typename P::real> (&acc)[12]) {
+  static_assert(REDUCE != RED_DOT_SELF || MODE == HOP_XPAY, "(out, self) needs the XPAY epilogue");
   using T = typename P::real;
   const Geom& g = a.g;
   const T coef = (T)a.a;
   cplx<T> out[12];
+  cplx<T> self[12];
   if constexpr (MODE == HOP_PLAIN) {
 #pragma unroll
     for (int k = 0; k < 12; ++k) out[k] = coef * acc[k];
@@ -464,7 +483,6 @@ __device__ __forceinline__ typename P::real hop_epilogue(const HopArgs& a, int r
       for (int k = 0; k < 6; ++k) out[6 * b + k] = y[k];
     }
   } else {  // HOP_XPAY
-    cplx<T> self[12];
     const char* sp = (const char*)a.self + (size_t)rhs * a.self_rhs_bytes;
     load_spinor<P>(self, sp, a.self_norm ? a.self_norm + (size_t)rhs * a.norm_rhs_stride : nullptr, idx, g.stride);
 #pragma unroll
@@ -495,16 +513,28 @@ __device__ __forceinline__ typename P::real hop_epilogue(const HopArgs& a, int r
   }
   char* op = (char*)a.out + (size_t)rhs * a.out_rhs_bytes;
   store_spinor<P>(op, a.out_norm ? a.out_norm + (size_t)rhs * a.norm_rhs_stride : nullptr, idx, g.stride, out);
-  T site = 0;
-  if constexpr (REDUCE) {
-    // site sum in the compute precision (FP64 is slow on this part), block sums in FP64
+  // site sums in the compute precision (FP64 is slow on this part), block sums in FP64
+  Sums3<T> site{{0, 0, 0}};
+  if constexpr (REDUCE != RED_NONE) {
+    T nn = 0;
 #pragma unroll
-    for (int k = 0; k < 12; ++k) site = fmadd(out[k].re, out[k].re, fmadd(out[k].im, out[k].im, site));
+    for (int k = 0; k < 12; ++k) nn = fmadd(out[k].re, out[k].re, fmadd(out[k].im, out[k].im, nn));
+    site.q[REDUCE == RED_DOT_SELF ? 2 : 0] = nn;
+  }
+  if constexpr (REDUCE == RED_DOT_SELF) {
+    T re = 0, im = 0;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      re = fmadd(out[k].re, self[k].re, fmadd(out[k].im, self[k].im, re));
+      im = fmadd(out[k].re, self[k].im, fmadd(-out[k].im, self[k].re, im));
+    }
+    site.q[0] = re;
+    site.q[1] = im;
   }
   return site;
 }
 
-template <typename P, int RECON, int MODE, bool DAG, bool REDUCE, int TX, int NRB, int MINB>
+template <typename P, int RECON, int MODE, bool DAG, int REDUCE, int TX, int NRB, int MINB>
 __global__ void __launch_bounds__(TX * NRB, MINB) hop_kernel(const HopArgs a) {
   const int ng = (a.nrhs + NRB - 1) / NRB;
   const int sblock = blockIdx.x / ng;
@@ -513,13 +543,13 @@ __global__ void __launch_bounds__(TX * NRB, MINB) hop_kernel(const HopArgs a) {
 
 // One launch over several independent lattices (each its own HopArgs: geometry, fields,
 // partials): block b works on lattice work[b].x, site block work[b].y.
-template <typename P, int RECON, int MODE, bool DAG, bool REDUCE>
+template <typename P, int RECON, int MODE, bool DAG, int REDUCE>
 __global__ void __launch_bounds__(128) hop_kernel_multi(const HopArgs* __restrict__ args, const int2* __restrict__ work) {
   const int2 w = work[blockIdx.x];
   hop_body<P, RECON, MODE, DAG, REDUCE, 128, 1>(args[w.x], w.y, 0);
 }
 
-template <typename P, int RECON, int MODE, bool DAG, bool REDUCE, int TX, int NRB>
+template <typename P, int RECON, int MODE, bool DAG, int REDUCE, int TX, int NRB>
 __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group) {
   using T = typename P::real;
   const int tid = threadIdx.x;
@@ -527,7 +557,7 @@ __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group
   const int rhs = group * NRB + rl;
   const int idx = sblock * TX + (tid % TX);
   const Geom& g = a.g;
-  const bool active = idx < g.Vh && rhs < a.nrhs;
+  const bool active = idx < g.Vh && rhs < a.nrhs && (!a.active || a.active[(size_t)rhs * a.active_stride]);
   // 8 x 9 x 32 x 16 B = 36 KiB of static shared memory for 32-site blocks
   constexpr bool kShared = NRB > 1 && TX == 32 && std::is_same<T, float>::value;
   __shared__ float4 lsm[kShared ? 8 : 1][9][kShared ? TX : 1];
@@ -536,8 +566,8 @@ __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group
     stage_links<P, RECON, TX>(lsm, nsm, a, sblock);
     __syncthreads();
   }
-  // |out|^2: thread and warp sums in the compute precision, block sums in FP64
-  T local = 0;
+  // fused reductions: thread and warp sums in the compute precision, block sums in FP64
+  Sums3<T> local{{0, 0, 0}};
   if (active) {
     Coord c = cb_coords(g, idx, a.out_parity);
     const char* in = (const char*)a.in + (size_t)rhs * a.in_rhs_bytes;
@@ -571,20 +601,50 @@ __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group
     }
     local = hop_epilogue<P, MODE, DAG, REDUCE>(a, rhs, idx, acc);
   }
-  if constexpr (REDUCE) {
+  if constexpr (REDUCE != RED_NONE) {
     // warps never straddle two right-hand sides (TX is a multiple of 32)
-    __shared__ double wsum[TX * NRB / 32];
+    constexpr int NQ = red_count<REDUCE>();
+    __shared__ double wsum[NQ][TX * NRB / 32];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
-    if ((tid & 31) == 0) wsum[tid >> 5] = (double)local;
+    for (int q = 0; q < NQ; ++q) {
+      T v = local.q[q];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+      if ((tid & 31) == 0) wsum[q][tid >> 5] = (double)v;
+    }
     __syncthreads();
     if (tid < NRB) {
       const int r = group * NRB + tid;
-      double s = 0.0;
 #pragma unroll
-      for (int w = 0; w < TX / 32; ++w) s += wsum[tid * (TX / 32) + w];
-      if (r < a.nrhs) a.partials[(size_t)r * a.part_stride + sblock] = s;
+      for (int q = 0; q < NQ; ++q) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < TX / 32; ++w) s += wsum[q][tid * (TX / 32) + w];
+        if (r < a.nrhs) a.partials[((size_t)q * a.nrhs + r) * a.part_stride + sblock] = s;
+      }
     }
+  }
+}
+
+// block sums of a one-right-hand-side block of NT threads (pair and ring kernels): partial rows
+// q * nrhs + rhs
+template <int NQ, int NT, typename T>
+__device__ __forceinline__ void block_sums_1rhs(const HopArgs& a, Sums3<T> local, int rhs, int sblock) {
+  __shared__ double wsum[NQ][NT / 32];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    T v = local.q[q];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) wsum[q][threadIdx.x >> 5] = (double)v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    const int q = threadIdx.x;
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) s += wsum[q][w];
+    a.partials[((size_t)q * a.nrhs + rhs) * a.part_stride + sblock] = s;
   }
 }
 
@@ -769,15 +829,15 @@ __device__ __forceinline__ void hop_dir_pair(C2 (&acc)[12], const HopArgs& a, co
 }
 
 // Grid: Vh/2 / TX site blocks x nrhs, right-hand sides fastest (as hop_kernel with NRB = 1).
-template <int RECON, int MODE, bool DAG, bool REDUCE, int TX, int MINB>
+template <int RECON, int MODE, bool DAG, int REDUCE, int TX, int MINB>
 __global__ void __launch_bounds__(TX, MINB) hop_kernel_pair(const HopArgs a) {
   const int sblock = blockIdx.x / a.nrhs;
   const int rhs = blockIdx.x - sblock * a.nrhs;
   const Geom& g = a.g;
   const int half = g.Vh >> 1;
   const int ia = sblock * TX + threadIdx.x;
-  float local = 0.f;  // thread and warp sums in FP32, block sums in FP64
-  if (ia < half) {
+  Sums3<float> local{{0.f, 0.f, 0.f}};  // thread and warp sums in FP32, block sums in FP64
+  if (ia < half && (!a.active || a.active[(size_t)rhs * a.active_stride])) {
     const int ib = ia + half;
     const Coord ca = cb_coords(g, ia, a.out_parity);
     Coord cb = ca;
@@ -798,22 +858,9 @@ __global__ void __launch_bounds__(TX, MINB) hop_kernel_pair(const HopArgs a) {
       sa[k] = {acc[k].r.x, acc[k].i.x};
       sb[k] = {acc[k].r.y, acc[k].i.y};
     }
-    local = hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, ia, sa);
-    local += hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, ib, sb);
+    local = hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, ia, sa) + hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, ib, sb);
   }
-  if constexpr (REDUCE) {
-    __shared__ double wsum[TX / 32];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)local;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0.0;
-#pragma unroll
-      for (int w = 0; w < TX / 32; ++w) s += wsum[w];
-      a.partials[(size_t)rhs * a.part_stride + sblock] = s;
-    }
-  }
+  if constexpr (REDUCE != RED_NONE) block_sums_1rhs<red_count<REDUCE>(), TX>(a, local, rhs, sblock);
 }
 
 }  // namespace gbc

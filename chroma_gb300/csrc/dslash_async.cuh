@@ -138,15 +138,15 @@ __device__ __forceinline__ void ring_step(float2 (&acc)[12], HopRing<RECON, TX>&
 }
 
 // Grid: Vh / TX site blocks x nrhs, right-hand sides fastest (as hop_kernel with NRB = 1).
-template <int RECON, int MODE, bool DAG, bool REDUCE, int TX, int MINB>
+template <int RECON, int MODE, bool DAG, int REDUCE, int TX, int MINB>
 __global__ void __launch_bounds__(TX, MINB) hop_kernel_async(const HopArgs a) {
   __shared__ HopRing<RECON, TX> R;
   const int sblock = blockIdx.x / a.nrhs;
   const int rhs = blockIdx.x - sblock * a.nrhs;
   const Geom& g = a.g;
   const int idx = sblock * TX + threadIdx.x;
-  float local = 0.f;  // thread and warp sums in FP32, block sums in FP64
-  if (idx < g.Vh) {
+  Sums3<float> local{{0.f, 0.f, 0.f}};  // thread and warp sums in FP32, block sums in FP64
+  if (idx < g.Vh && (!a.active || a.active[(size_t)rhs * a.active_stride])) {
     const Coord c = cb_coords(g, idx, a.out_parity);
     const HopSites hs = hop_sites(g, c);
     const char* in = (const char*)a.in + (size_t)rhs * a.in_rhs_bytes;
@@ -169,19 +169,7 @@ __global__ void __launch_bounds__(TX, MINB) hop_kernel_async(const HopArgs a) {
     for (int k = 0; k < 12; ++k) out[k] = {acc[k].x, acc[k].y};
     local = hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, rhs, idx, out);
   }
-  if constexpr (REDUCE) {
-    __shared__ double wsum[TX / 32];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xffffffffu, local, off);
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = (double)local;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0.0;
-#pragma unroll
-      for (int w = 0; w < TX / 32; ++w) s += wsum[w];
-      a.partials[(size_t)rhs * a.part_stride + sblock] = s;
-    }
-  }
+  if constexpr (REDUCE != RED_NONE) block_sums_1rhs<red_count<REDUCE>(), TX>(a, local, rhs, sblock);
 }
 
 }  // namespace gbc

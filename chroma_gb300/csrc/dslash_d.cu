@@ -2,16 +2,16 @@
 #include "gbc_kernels.h"
 
 namespace gbc {
-int hop_launch_d0(int recon, int mode, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
-int hop_launch_d1(int recon, int mode, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
-int hop_multi_launch_d0(int recon, int mode, bool reduce, const HopArgs* args, const int2* work, int nwork,
+int hop_launch_d0(int recon, int mode, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+int hop_launch_d1(int recon, int mode, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+int hop_multi_launch_d0(int recon, int mode, int reduce, const HopArgs* args, const int2* work, int nwork,
                           cudaStream_t s);
-int hop_multi_launch_d1(int recon, int mode, bool reduce, const HopArgs* args, const int2* work, int nwork,
+int hop_multi_launch_d1(int recon, int mode, int reduce, const HopArgs* args, const int2* work, int nwork,
                           cudaStream_t s);
-int hop_launch_d(int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
+int hop_launch_d(int recon, int mode, bool dag, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
   return dag ? hop_launch_d1(recon, mode, reduce, a, sh, s) : hop_launch_d0(recon, mode, reduce, a, sh, s);
 }
-int hop_multi_launch_d(int recon, int mode, bool dag, bool reduce, const HopArgs* args, const int2* work, int nwork,
+int hop_multi_launch_d(int recon, int mode, bool dag, int reduce, const HopArgs* args, const int2* work, int nwork,
                          cudaStream_t s) {
   return dag ? hop_multi_launch_d1(recon, mode, reduce, args, work, nwork, s)
              : hop_multi_launch_d0(recon, mode, reduce, args, work, nwork, s);

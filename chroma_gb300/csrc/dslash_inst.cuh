@@ -8,7 +8,7 @@
 
 namespace gbc {
 
-template <typename P, int RECON, int MODE, bool DAG, bool REDUCE>
+template <typename P, int RECON, int MODE, bool DAG, int REDUCE>
 static int hop_shape(const HopArgs& a, HopShape sh, cudaStream_t s) {
   const int nbx = (a.g.Vh + sh.tx - 1) / sh.tx;
   auto go = [&](auto kern, int tx, int nrb) {
@@ -72,19 +72,24 @@ static int hop_shape(const HopArgs& a, HopShape sh, cudaStream_t s) {
 }
 
 template <typename P, int RECON, bool DAG>
-static int hop_mode(int mode, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
+static int hop_mode(int mode, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
   switch (mode) {
-    case HOP_PLAIN: return hop_shape<P, RECON, HOP_PLAIN, DAG, false>(a, sh, s);
-    case HOP_CLOV: return hop_shape<P, RECON, HOP_CLOV, DAG, false>(a, sh, s);
+    case HOP_PLAIN: return reduce ? -1 : hop_shape<P, RECON, HOP_PLAIN, DAG, RED_NONE>(a, sh, s);
+    case HOP_CLOV: return reduce ? -1 : hop_shape<P, RECON, HOP_CLOV, DAG, RED_NONE>(a, sh, s);
     case HOP_XPAY:
-      return reduce ? hop_shape<P, RECON, HOP_XPAY, DAG, true>(a, sh, s)
-                    : hop_shape<P, RECON, HOP_XPAY, DAG, false>(a, sh, s);
+      if (reduce == RED_NORM) return hop_shape<P, RECON, HOP_XPAY, DAG, RED_NORM>(a, sh, s);
+      if (reduce == RED_DOT_SELF) {
+        // BiCGStab applies M~ itself, never its dagger: the variant exists for isign = PLUS only
+        if constexpr (!DAG) return hop_shape<P, RECON, HOP_XPAY, DAG, RED_DOT_SELF>(a, sh, s);
+        return -1;
+      }
+      return hop_shape<P, RECON, HOP_XPAY, DAG, RED_NONE>(a, sh, s);
   }
   return -1;
 }
 
 template <typename P, bool DAG>
-static int hop_recon(int recon, int mode, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
+static int hop_recon(int recon, int mode, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
   if (recon == 18) return hop_mode<P, 18, DAG>(mode, reduce, a, sh, s);
 #if GBC_RECON12
   if (recon == 12) return hop_mode<P, 12, DAG>(mode, reduce, a, sh, s);
@@ -94,20 +99,21 @@ static int hop_recon(int recon, int mode, bool reduce, const HopArgs& a, HopShap
 
 // several lattices in one launch (work table of (lattice, site block), 128-site blocks)
 template <typename P, int RECON, bool DAG>
-static int hop_multi_mode(int mode, bool reduce, const HopArgs* args, const int2* work, int nwork, cudaStream_t s) {
+static int hop_multi_mode(int mode, int reduce, const HopArgs* args, const int2* work, int nwork, cudaStream_t s) {
   switch (mode) {
-    case HOP_PLAIN: hop_kernel_multi<P, RECON, HOP_PLAIN, DAG, false><<<nwork, 128, 0, s>>>(args, work); return nwork;
-    case HOP_CLOV: hop_kernel_multi<P, RECON, HOP_CLOV, DAG, false><<<nwork, 128, 0, s>>>(args, work); return nwork;
+    case HOP_PLAIN: hop_kernel_multi<P, RECON, HOP_PLAIN, DAG, RED_NONE><<<nwork, 128, 0, s>>>(args, work); return nwork;
+    case HOP_CLOV: hop_kernel_multi<P, RECON, HOP_CLOV, DAG, RED_NONE><<<nwork, 128, 0, s>>>(args, work); return nwork;
     case HOP_XPAY:
-      if (reduce) hop_kernel_multi<P, RECON, HOP_XPAY, DAG, true><<<nwork, 128, 0, s>>>(args, work);
-      else hop_kernel_multi<P, RECON, HOP_XPAY, DAG, false><<<nwork, 128, 0, s>>>(args, work);
+      if (reduce == RED_DOT_SELF) return -1;
+      if (reduce) hop_kernel_multi<P, RECON, HOP_XPAY, DAG, RED_NORM><<<nwork, 128, 0, s>>>(args, work);
+      else hop_kernel_multi<P, RECON, HOP_XPAY, DAG, RED_NONE><<<nwork, 128, 0, s>>>(args, work);
       return nwork;
   }
   return -1;
 }
 
 template <typename P, bool DAG>
-static int hop_multi_recon(int recon, int mode, bool reduce, const HopArgs* args, const int2* work, int nwork,
+static int hop_multi_recon(int recon, int mode, int reduce, const HopArgs* args, const int2* work, int nwork,
                            cudaStream_t s) {
   if (recon == 18) return hop_multi_mode<P, 18, DAG>(mode, reduce, args, work, nwork, s);
 #if GBC_RECON12

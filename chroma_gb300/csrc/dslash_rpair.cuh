@@ -136,31 +136,40 @@ __device__ __forceinline__ void hop_dir_rp(C2 (&acc)[12], const float4 (*lsm)[9]
   }
 }
 
-// |out|^2 partials of a two-RHS block: lanes of one parity share a pair group, so a butterfly over
-// the even lane offsets leaves the even-lane sums in lane 0 and the odd-lane sums in lane 1; then a
-// fixed-order sum over the TS/16 warps of each pair group (bitwise repeatable)
-template <int TS, int NRB>
-__device__ __forceinline__ void rp_block_sums(const HopArgs& a, float l0, float l1, int group, int sblock) {
+// fused-reduction partials of a two-RHS block: lanes of one parity share a pair group, so a
+// butterfly over the even lane offsets leaves the even-lane sums in lane 0 and the odd-lane sums in
+// lane 1; then a fixed-order sum over the TS/16 warps of each pair group (bitwise repeatable).
+// Partial rows q * nrhs + rhs.
+template <int TS, int NRB, int NQ>
+__device__ __forceinline__ void rp_block_sums(const HopArgs& a, Sums3<float> l0, Sums3<float> l1, int group,
+                                              int sblock) {
   constexpr int SW = TS / 16;
   const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-  __shared__ double wsum[TS * NRB / 64][2][2];
+  __shared__ double wsum[NQ][TS * NRB / 64][2][2];
 #pragma unroll
-  for (int off = 16; off >= 2; off >>= 1) {
-    l0 += __shfl_xor_sync(0xffffffffu, l0, off);
-    l1 += __shfl_xor_sync(0xffffffffu, l1, off);
-  }
-  if (l < 2) {
-    wsum[w][l][0] = (double)l0;
-    wsum[w][l][1] = (double)l1;
+  for (int q = 0; q < NQ; ++q) {
+    float v0 = l0.q[q], v1 = l1.q[q];
+#pragma unroll
+    for (int off = 16; off >= 2; off >>= 1) {
+      v0 += __shfl_xor_sync(0xffffffffu, v0, off);
+      v1 += __shfl_xor_sync(0xffffffffu, v1, off);
+    }
+    if (l < 2) {
+      wsum[q][w][l][0] = (double)v0;
+      wsum[q][w][l][1] = (double)v1;
+    }
   }
   __syncthreads();
   if (tid < NRB) {
-    const int q = tid >> 1;
+    const int pgp = tid >> 1;
     const int r = group * NRB + tid;
-    double sum = 0.0;
 #pragma unroll
-    for (int k = 0; k < SW; ++k) sum += wsum[(q >> 1) * SW + k][q & 1][tid & 1];
-    if (r < a.nrhs) a.partials[(size_t)r * a.part_stride + sblock] = sum;
+    for (int q = 0; q < NQ; ++q) {
+      double sum = 0.0;
+#pragma unroll
+      for (int k = 0; k < SW; ++k) sum += wsum[q][(pgp >> 1) * SW + k][pgp & 1][tid & 1];
+      if (r < a.nrhs) a.partials[((size_t)q * a.nrhs + r) * a.part_stride + sblock] = sum;
+    }
   }
 }
 
@@ -168,7 +177,7 @@ __device__ __forceinline__ void rp_block_sums(const HopArgs& a, float l0, float 
 // Grid: ceil(Vh / TS) site blocks x ceil(nrhs / NRB) right-hand-side groups, groups fastest.
 // Thread t: warp w = t / 32, lane l; site (w % (TS/16)) * 16 + l / 2 of the block, pair group
 // (w / (TS/16)) * 2 + (l & 1), i.e. right-hand sides 2 pg and 2 pg + 1 of the group.
-template <int RECON, int MODE, bool DAG, bool REDUCE, int TS, int NRB, int MINB>
+template <int RECON, int MODE, bool DAG, int REDUCE, int TS, int NRB, int MINB>
 __global__ void __launch_bounds__(TS * NRB / 2, MINB) hop_kernel_rp(const HopArgs a) {
   static_assert(TS % 16 == 0 && NRB % 4 == 0, "TS sites in half-warps, pair groups in lane pairs");
   constexpr int SW = TS / 16;
@@ -185,8 +194,11 @@ __global__ void __launch_bounds__(TS * NRB / 2, MINB) hop_kernel_rp(const HopArg
   __shared__ int nsm[8][TS];
   stage_links_rp<RECON, TS>(lsm, nsm, a, sblock);
   __syncthreads();
-  float l0 = 0.f, l1 = 0.f;  // thread and warp sums in FP32, block sums in FP64
-  if (idx < g.Vh && r0 < a.nrhs) {
+  Sums3<float> l0{{0.f, 0.f, 0.f}}, l1{{0.f, 0.f, 0.f}};  // thread and warp sums in FP32, block sums in FP64
+  // a pair with one live right-hand side computes both (the other's output is simply refreshed)
+  const bool live = r0 < a.nrhs && (!a.active || a.active[(size_t)r0 * a.active_stride] ||
+                                    a.active[(size_t)(r0 + 1) * a.active_stride]);
+  if (idx < g.Vh && live) {
     const char* in0 = (const char*)a.in + (size_t)r0 * a.in_rhs_bytes;
     const char* in1 = in0 + a.in_rhs_bytes;
     const float* nm0 = a.in_norm + (size_t)r0 * a.norm_rhs_stride;
@@ -207,7 +219,7 @@ __global__ void __launch_bounds__(TS * NRB / 2, MINB) hop_kernel_rp(const HopArg
     l0 = hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, r0, idx, sa);
     l1 = hop_epilogue<PrecH, MODE, DAG, REDUCE>(a, r0 + 1, idx, sb);
   }
-  if constexpr (REDUCE) rp_block_sums<TS, NRB>(a, l0, l1, group, sblock);
+  if constexpr (REDUCE != RED_NONE) rp_block_sums<TS, NRB, red_count<REDUCE>()>(a, l0, l1, group, sblock);
 }
 
 }  // namespace gbc

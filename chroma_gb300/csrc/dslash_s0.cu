@@ -3,10 +3,10 @@
 #include "dslash_inst.cuh"
 
 namespace gbc {
-int hop_launch_s0(int recon, int mode, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
+int hop_launch_s0(int recon, int mode, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
   return hop_recon<PrecS, false>(recon, mode, reduce, a, sh, s);
 }
-int hop_multi_launch_s0(int recon, int mode, bool reduce, const HopArgs* args, const int2* work, int nwork,
+int hop_multi_launch_s0(int recon, int mode, int reduce, const HopArgs* args, const int2* work, int nwork,
                           cudaStream_t s) {
   return hop_multi_recon<PrecS, false>(recon, mode, reduce, args, work, nwork, s);
 }

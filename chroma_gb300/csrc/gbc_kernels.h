@@ -11,6 +11,9 @@ void count_launch(long long n = 1);
 long long launch_count();
 
 enum { HOP_PLAIN = 0, HOP_CLOV = 1, HOP_XPAY = 2 };
+// reductions fused into the stencil epilogue: none; |out|^2; (out, self) and |out|^2 of the XPAY
+// epilogue (BiCGStab's (t, s), (t, t) for t = M~ s), three partial rows per right-hand side
+enum { RED_NONE = 0, RED_NORM = 1, RED_DOT_SELF = 2 };
 enum { PREC_HALF = 2, PREC_SINGLE = 4, PREC_DOUBLE = 8 };
 
 struct Geom {
@@ -51,8 +54,12 @@ struct HopArgs {
   const void* clov;          // packed clover of the output parity (HOP_CLOV, HOP_XPAY)
   double a;                  // coefficient of D' psi
   double twist;              // HOP_XPAY: twisted-mass mu (0 = none)
-  double* partials;          // REDUCE: |out|^2 per block, [rhs][part_stride]
+  double* partials;          // RED_*: sums per block, [quantity][rhs][part_stride]
   int part_stride;
+  // optional per-right-hand-side flags (active[r * active_stride] != 0): a right-hand side whose
+  // flag is 0 is skipped (no loads, no store, zero partials); nullptr = all active
+  const int* active;
+  int active_stride;
 };
 
 // Launch geometry chosen by the caller (autotuned): TX sites x NRB right-hand sides per block,
@@ -90,18 +97,18 @@ inline int hop_blocks(const HopShape& sh, int Vh) {
 
 // Returns the number of x-blocks launched (partials per right-hand side), or -1 if the
 // (precision, recon, shape) combination is not compiled.
-int hop_launch_d(int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
-int hop_launch_s(int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
-int hop_launch_h(int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+int hop_launch_d(int recon, int mode, bool dag, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+int hop_launch_s(int recon, int mode, bool dag, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+int hop_launch_h(int recon, int mode, bool dag, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
 
 // One launch over several lattices: args[l] in device memory, work[b] = (lattice, 128-site block).
-int hop_multi_launch_d(int recon, int mode, bool dag, bool reduce, const HopArgs* args, const int2* work, int nwork,
+int hop_multi_launch_d(int recon, int mode, bool dag, int reduce, const HopArgs* args, const int2* work, int nwork,
                        cudaStream_t s);
-int hop_multi_launch_s(int recon, int mode, bool dag, bool reduce, const HopArgs* args, const int2* work, int nwork,
+int hop_multi_launch_s(int recon, int mode, bool dag, int reduce, const HopArgs* args, const int2* work, int nwork,
                        cudaStream_t s);
-int hop_multi_launch_h(int recon, int mode, bool dag, bool reduce, const HopArgs* args, const int2* work, int nwork,
+int hop_multi_launch_h(int recon, int mode, bool dag, int reduce, const HopArgs* args, const int2* work, int nwork,
                        cudaStream_t s);
-inline int hop_multi_launch(int prec, int recon, int mode, bool dag, bool reduce, const HopArgs* args,
+inline int hop_multi_launch(int prec, int recon, int mode, bool dag, int reduce, const HopArgs* args,
                             const int2* work, int nwork, cudaStream_t s) {
   switch (prec) {
     case PREC_DOUBLE: return hop_multi_launch_d(recon, mode, dag, reduce, args, work, nwork, s);
@@ -111,7 +118,7 @@ inline int hop_multi_launch(int prec, int recon, int mode, bool dag, bool reduce
   return -1;
 }
 
-inline int hop_launch(int prec, int recon, int mode, bool dag, bool reduce, const HopArgs& a, HopShape sh,
+inline int hop_launch(int prec, int recon, int mode, bool dag, int reduce, const HopArgs& a, HopShape sh,
                       cudaStream_t s) {
   switch (prec) {
     case PREC_DOUBLE: return hop_launch_d(recon, mode, dag, reduce, a, sh, s);
