@@ -205,3 +205,30 @@ def test_multi_rhs_solve_point_sources(setup):
     for k in (0, 5, 11):
         r = op.apply(O.OP_UNPREC, psi[k]) - src[k]
         assert np.linalg.norm(r) / np.linalg.norm(src[k]) < 1e-9
+
+
+@pytest.mark.parametrize("sloppy", [G.PREC_HALF, G.PREC_SINGLE], ids=["fp16", "fp32"])
+def test_bicgstab_tight_target(sloppy):
+    """A 1e-12 target with the inner BiCGStab: the inner solves stop at their accumulators' floor
+    (or break down and hand over to the inner CGNE) and the FP64 outer loop still reaches the
+    target for every right-hand side of a 4-source batch."""
+    from oracle import Oracle, OracleOp
+    from oracle import oracle as O
+    o = Oracle()
+    kappa, csw = 0.124, 1.5
+    mass = 1 / (2 * kappa) - 4
+    dims = (4, 6, 8, 10)
+    u = o.apply_bc(dims, o.gauge_hot(dims, 0.3, 503), (1, 1, 1, -1))
+    op = OracleOp(dims, u, mass, csw)
+    chi = np.stack([S.z2_noise(dims, 610 + k, cb=1).reshape(-1, 12) for k in range(4)])
+    ctx = G.Context(dims, mass, csw, t_boundary=-1, max_rhs=4, sloppy_precision=sloppy)
+    try:
+        ctx.load_gauge(u)
+        psi, res, rc = ctx.solve(chi, solver=G.SOLVER_BICGSTAB, rsd_target=1e-12, delta=0.01)
+        assert rc == 0, res
+        for k in range(4):
+            r = chi[k] - op.apply(O.OP_MEO, psi[k])
+            assert np.sqrt(op.norm2(r) / op.norm2(chi[k])) <= 1.05e-12, (k, res[k])
+            assert res[k]["status"] == 0
+    finally:
+        ctx.close()
