@@ -427,6 +427,7 @@ void gbc_destroy(gbc_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_ctx_memory(c);
   precond_free(c);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -595,9 +596,28 @@ int gbc_solve(gbc_ctx* c, const gbc_solve_params* p, int nrhs, double* psi, cons
     // only a zero-guess solve of the full system overwrites every site without reading psi
     if (!(p->zero_guess && p->system == GBC_SYS_FULL))
       GBC_CUDA(cudaMemcpyAsync(c->d_stage[1], psi, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    int rc = solve_device(c, p, nrhs, c->d_stage[1], c->d_stage[0], res);
-    GBC_CUDA(cudaMemcpyAsync(psi, c->d_stage[1], n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    // the solution's copy to the host runs on a second stream as soon as the solution is final,
+    // overlapping the FP64 residual check that only reads it
+    if (!c->copy_stream) GBC_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    cudaEvent_t exported;
+    GBC_CUDA(cudaEventCreateWithFlags(&exported, cudaEventDisableTiming));
+    // (a call refused before the solve starts leaves psi untouched)
+    const std::function<void()> d2h = [&]() {
+      GBC_CUDA(cudaEventRecord(exported, c->stream));
+      GBC_CUDA(cudaStreamWaitEvent(c->copy_stream, exported, 0));
+      GBC_CUDA(cudaMemcpyAsync(psi, c->d_stage[1], n * sizeof(double), cudaMemcpyDeviceToHost, c->copy_stream));
+    };
+    int rc;
+    try {
+      rc = solve_device(c, p, nrhs, c->d_stage[1], c->d_stage[0], res, &d2h);
+    } catch (...) {
+      cudaStreamSynchronize(c->copy_stream);
+      cudaEventDestroy(exported);
+      throw;
+    }
     sync(c);
+    GBC_CUDA(cudaStreamSynchronize(c->copy_stream));
+    cudaEventDestroy(exported);
     double t1 = now();
     for (int r = 0; r < nrhs; ++r) res[r].seconds = t1 - t0;
     return rc;

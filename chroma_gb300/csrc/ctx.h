@@ -5,6 +5,7 @@
 
 #include <chrono>
 #include <cstdio>
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -104,6 +105,8 @@ struct gbc_ctx {
   // inner BiCGStab points them at its scalars so that converged right-hand sides cost nothing
   const int* hop_active = nullptr;
   int hop_active_stride = 0;
+  // second stream for the host copies of gbc_solve that overlap device work (created on first use)
+  cudaStream_t copy_stream = nullptr;
 };
 
 namespace gbc {
@@ -153,7 +156,9 @@ InnerStats bicgstab(gbc_ctx* c, int pa, int po, double tol, int maxit, double de
                     const Spinor& b, const std::vector<int>& active);
 
 // ---- solvers (solvers.cu) -------------------------------------------------------------------
+// after_export (optional) runs once the solution is in psi_canon on the context stream and before
+// the final residual check, which only reads it: gbc_solve starts the copy to the host there
 int solve_device(gbc_ctx* c, const gbc_solve_params* p, int nrhs, double* psi_canon, const double* chi_canon,
-                 gbc_result* res);
+                 gbc_result* res, const std::function<void()>* after_export = nullptr);
 
 }  // namespace gbc

@@ -511,7 +511,7 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
 }  // namespace
 
 int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_canon, const double* chi_canon,
-                 gbc_result* res) {
+                 gbc_result* res, const std::function<void()>* after_export) {
   gbc_solve_params p = *pp;
   if (!(p.rsd_target > 0)) p.rsd_target = 1e-10;
   if (p.max_iter <= 0) p.max_iter = 10000;
@@ -813,12 +813,14 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     }
   }
   export_spinor(g, psi_canon, rs, 1, psi, s);
+  if (p.system != GBC_SYS_FULL && after_export) (*after_export)();
   if (p.system == GBC_SYS_FULL) {
     // psi_e = A_ee^-1 (chi_e + 1/2 D_eo psi_o)   (eoprec_fermact_qprop.cc:60-67)
     hop(c, D, 0, HOP_PLAIN, false, 0.5, psi, t1, nullptr, nullptr, false);
     blas_xpy(g, t1, chie, s);
     apply_clover(c, D, 0, true, t1, psie);
     export_spinor(g, psi_canon, rs, 0, psie, s);
+    if (after_export) (*after_export)();
     // full residual |M psi - chi| over both parities (eoprec_fermact_qprop.cc:70-76); the even
     // part A_ee psi_e - 1/2 D_eo psi_o - chi_e reuses t1 = chi_e + 1/2 D_eo psi_o from above
     Spinor ue = sub(workspace(c, SLOT_T2 + 50, D, n), 0, n);
