@@ -456,6 +456,36 @@ __device__ __forceinline__ Sums3<T> operator+(Sums3<T> a, const Sums3<T>& b) {
   return a;
 }
 
+// Store one output site in the output precision and return its site sums of the REDUCE kind
+// (self: the XPAY operand, for RED_DOT_SELF).
+template <typename P, int REDUCE>
+__device__ __forceinline__ Sums3<typename P::real> store_site(const HopArgs& a, int rhs, int idx,
+                                                              const cplx<typename P::real> (&out)[12],
+                                                              const cplx<typename P::real> (&self)[12]) {
+  using T = typename P::real;
+  char* op = (char*)a.out + (size_t)rhs * a.out_rhs_bytes;
+  store_spinor<P>(op, a.out_norm ? a.out_norm + (size_t)rhs * a.norm_rhs_stride : nullptr, idx, a.g.stride, out);
+  // site sums in the compute precision (FP64 is slow on this part), block sums in FP64
+  Sums3<T> site{{0, 0, 0}};
+  if constexpr (REDUCE != RED_NONE) {
+    T nn = 0;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) nn = fmadd(out[k].re, out[k].re, fmadd(out[k].im, out[k].im, nn));
+    site.q[REDUCE == RED_DOT_SELF ? 2 : 0] = nn;
+  }
+  if constexpr (REDUCE == RED_DOT_SELF) {
+    T re = 0, im = 0;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      re = fmadd(out[k].re, self[k].re, fmadd(out[k].im, self[k].im, re));
+      im = fmadd(out[k].re, self[k].im, fmadd(-out[k].im, self[k].re, im));
+    }
+    site.q[0] = re;
+    site.q[1] = im;
+  }
+  return site;
+}
+
 // The MODE epilogue of one output site: out = a D' psi, T (a D' psi) or T self + a D' psi
 // (+ twist), stored in the output precision; returns the site sums of the REDUCE kind.
 template <typename P, int MODE, bool DAG, int REDUCE>
@@ -511,27 +541,7 @@ __device__ __forceinline__ Sums3<typename P::real> hop_epilogue(const HopArgs& a
       }
     }
   }
-  char* op = (char*)a.out + (size_t)rhs * a.out_rhs_bytes;
-  store_spinor<P>(op, a.out_norm ? a.out_norm + (size_t)rhs * a.norm_rhs_stride : nullptr, idx, g.stride, out);
-  // site sums in the compute precision (FP64 is slow on this part), block sums in FP64
-  Sums3<T> site{{0, 0, 0}};
-  if constexpr (REDUCE != RED_NONE) {
-    T nn = 0;
-#pragma unroll
-    for (int k = 0; k < 12; ++k) nn = fmadd(out[k].re, out[k].re, fmadd(out[k].im, out[k].im, nn));
-    site.q[REDUCE == RED_DOT_SELF ? 2 : 0] = nn;
-  }
-  if constexpr (REDUCE == RED_DOT_SELF) {
-    T re = 0, im = 0;
-#pragma unroll
-    for (int k = 0; k < 12; ++k) {
-      re = fmadd(out[k].re, self[k].re, fmadd(out[k].im, self[k].im, re));
-      im = fmadd(out[k].re, self[k].im, fmadd(-out[k].im, self[k].re, im));
-    }
-    site.q[0] = re;
-    site.q[1] = im;
-  }
-  return site;
+  return store_site<P, REDUCE>(a, rhs, idx, out, self);
 }
 
 template <typename P, int RECON, int MODE, bool DAG, int REDUCE, int TX, int NRB, int MINB>

@@ -232,3 +232,39 @@ def test_bicgstab_tight_target(sloppy):
             assert res[k]["status"] == 0
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("prec", [G.PREC_DOUBLE, G.PREC_SINGLE, G.PREC_HALF], ids=["f64", "f32", "f16"])
+def test_twisted_mass_operator_and_solve(prec):
+    """TwistedM of the clover XML: M~ with + isign i mu gamma_5 on the odd sites, 1 and 12
+    right-hand sides (so every compiled epilogue that carries the term runs), both isigns, and a
+    12-RHS solve to the oracle operator's FP64 true residual 1e-10."""
+    from oracle import Oracle, OracleOp
+    from oracle import oracle as O
+    dims, mu = (4, 6, 4, 8), 0.05
+    o = Oracle()
+    u = o.apply_bc(dims, o.gauge_hot(dims, 0.3, 4242), (1, 1, 1, -1))
+    mass = 1 / (2 * KAPPA) - 4
+    op = OracleOp(dims, u, mass, CSW, twisted_m=mu)
+    ctx = G.Context(dims, mass, CSW, t_boundary=-1, max_rhs=12, twisted_m=mu)
+    try:
+        ctx.load_gauge(u)
+        V = int(np.prod(dims))
+        par = S.parity(dims)
+        xs = np.stack([S.gaussian(dims, 80 + k).reshape(V, 12) for k in range(12)])
+        for isign in (1, -1):
+            want = [op.apply(O.OP_MEO, xs[k], isign, 1) for k in range(12)]
+            for n in (1, 12):
+                got = ctx.apply(G.OP_MEO, xs[:n], isign, 1, prec)
+                for k in range(n):
+                    assert rel(got[k][par == 1], want[k][par == 1]) < TOL[prec], (prec, isign, n, k)
+        if prec == G.PREC_HALF:
+            chi = np.stack([S.z2_noise(dims, 90 + k, cb=1).reshape(-1, 12) for k in range(12)])
+            for solver in (G.SOLVER_MIXED, G.SOLVER_BICGSTAB):
+                psi, res, rc = ctx.solve(chi, solver=solver, rsd_target=1e-10, delta=0.01)
+                assert rc == 0, res
+                for k in range(12):
+                    r = chi[k] - op.apply(O.OP_MEO, psi[k])
+                    assert np.sqrt(op.norm2(r) / op.norm2(chi[k])) <= 1.05e-10, (solver, k)
+    finally:
+        ctx.close()
