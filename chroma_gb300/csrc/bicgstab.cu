@@ -8,12 +8,15 @@
 //
 // The operator and the vectors it reads (p, v, s, t) are in the sloppy precision; x, r and the
 // shadow residual r0 in the accumulator precision (an fp16 r0 made the iteration counts of the
-// right-hand sides spread and cost more reliable updates than its bandwidth saved).  x and r are updated from the accumulator-precision r of
-// the step before (x += alpha p + omega (r - alpha v), r -= alpha v + omega t), so the sloppy copy
-// of s only feeds the operator and the (t, s) product.  Every scalar lives on the device (one thread
-// per right-hand side), so iterations replay from CUDA graphs; the host looks at the scalars every
-// few iterations for reliable updates (r = b - A x with the accumulator-precision operator), for
-// stalls at the accumulator precision's floor, and for convergence.
+// right-hand sides spread and cost more reliable updates than its bandwidth saved).  x and r are
+// updated from the accumulator-precision r of the step before (x += alpha p + omega (r - alpha v),
+// r -= alpha v + omega t), so the sloppy copy of s only feeds the operator and the (t, s) product,
+// which the stencil launch that writes t sums in its epilogue.  Every scalar lives on the device
+// (one thread per right-hand side), so iterations replay from CUDA graphs; the host looks at the
+// scalars every few iterations for reliable updates (r = b - A x with the accumulator-precision
+// operator), for stalls at the accumulator precision's floor, and for convergence.  A right-hand
+// side that has converged is skipped by every kernel of the iteration (its device flag), so the
+// batch's slowest sources do not make the others pay.
 #include <cmath>
 #include <cstring>
 
