@@ -75,6 +75,14 @@ def op_only(args):
                 "dslash64": (G.OP_DSLASH, G.PREC_DOUBLE), "meo16": (G.OP_MEO, G.PREC_HALF),
                 "meo64": (G.OP_MEO, G.PREC_DOUBLE)}[args.op_only]
     sec, byts = ctx.time_operator(op, prec, nrhs=args.nrhs, iters=args.iters, flush_l2=True)
+    if args.profile_timed:
+        # a second, tuned run inside cudaProfilerStart/Stop (ncu --profile-from-start off)
+        import torch
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        sec, byts = ctx.time_operator(op, prec, nrhs=args.nrhs, iters=args.iters, flush_l2=True)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     print(json.dumps({"op": args.op_only, "dims": dims, "nrhs": args.nrhs, "seconds": sec, "bytes": byts,
                       "GBps": byts / sec / 1e9, "tuned": ctx.tune_report().strip().splitlines()}), flush=True)
     ctx.close()
@@ -414,24 +422,28 @@ def main():
         plain_bicg = {"seconds": res[0]["device_seconds"], "iterations_per_rhs": res[0]["n_count"],
                       "true_rel_resid_max": max(r["rel_resid"] for r in res), "rc": rc}
 
-    # Dslash roofline: the FP16 12-RHS hopping kernel (dominant), cold L2 per launch
+    # Roofline of the dominant kernel pair: the FP16 M~ on 12 RHS (the A_ee^-1 D_eo and the
+    # A_oo x - 1/4 D_oe t launches the solve runs twice per iteration, 40 % of its time), cold L2
+    # per application, autotuned shapes as in the solve; algorithmic bytes Vh (16L + 2C + 5*12 S)
     pk, pk_kind = peaks()
-    sec, byts = ctx.time_operator(G.OP_DSLASH, G.PREC_HALF, nrhs=12, iters=20, flush_l2=True)
+    sec, byts = ctx.time_operator(G.OP_MEO, G.PREC_HALF, nrhs=12, iters=20, flush_l2=True)
+    secd, bytd = ctx.time_operator(G.OP_DSLASH, G.PREC_HALF, nrhs=12, iters=20, flush_l2=True)
     sec1, byts1 = ctx.time_operator(G.OP_DSLASH, G.PREC_HALF, nrhs=1, iters=20, flush_l2=True)
-    # the whole even-odd operator M~ (two fused launches, clover epilogues), one RHS, FP16:
-    # algorithmic bytes Vh (16L + 2C + 5S)
     secm, bytm = ctx.time_operator(G.OP_MEO, G.PREC_HALF, nrhs=1, iters=20, flush_l2=True)
     sec64, byts64 = ctx.time_operator(G.OP_DSLASH, G.PREC_DOUBLE, nrhs=1, iters=10, flush_l2=True)
     achieved = byts / sec / 1e9
-    # DRAM traffic of this launch: ncu dram__bytes_read.sum + dram__bytes_write.sum of the same
-    # kernel on 24^3x48 (456.7 MB for Vh = 331776 sites, 12 RHS), scaled to this lattice by the
-    # number of sites (profiles/hop_kernel_fp16_12rhs_24x24x24x48.md)
-    traffic = 456.7e6 / 331776 * (V // 2)
+    # DRAM traffic of one such M~: ncu dram__bytes_read.sum + dram__bytes_write.sum of its two
+    # launches on 24^3x48 (1228.1 MB for Vh = 331776 sites, 12 RHS), scaled to this lattice by the
+    # number of sites (profiles/launches_propagator_32x32x32x64.md)
+    traffic = 1228.1e6 / 331776 * (V // 2)
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"], "traffic": traffic, "traffic_source": "ncu, 24^3x48 scaled by sites",
             "peak_kind": pk_kind,
-            "kernel": "hop_kernel<PrecH,12,HOP_PLAIN> 12 RHS (Dslash, FP16 storage, 12-real links)",
+            "kernel": "M~ on 12 RHS, FP16 storage, 12-real links: hop_kernel_rp (A_ee^-1 D_eo) + hop_kernel_async "
+                      "(A_oo x - 1/4 D_oe t), autotuned",
+            "unit_of_work": "one M~ application (its two stencil launches)",
             "bytes_per_launch": byts, "seconds_per_launch": sec,
+            "dslash_12rhs_fp16_gbs": bytd / secd / 1e9, "dslash_12rhs_fp16_frac": bytd / secd / 1e9 / pk["hbm_gbs"],
             "single_rhs_fp16_gbs": byts1 / sec1 / 1e9, "single_rhs_fp16_frac": byts1 / sec1 / 1e9 / pk["hbm_gbs"],
             "single_rhs_meo_fp16_gbs": bytm / secm / 1e9, "single_rhs_meo_fp16_frac": bytm / secm / 1e9 / pk["hbm_gbs"],
             "single_rhs_fp64_gbs": byts64 / sec64 / 1e9}
