@@ -66,7 +66,9 @@ extern "C" {
                                      preconditioned by the learned network when loaded               */
 #define GBC_SOLVER_BICGSTAB 4     /* FP64 defect correction around a reliable BiCGStab on M~ in the
                                      sloppy precision: RELIABLE_BICGSTAB_MP_CLOVER_INVERTER
-                                     (reliable_bicgstab.cc:93-277), QUDA SolverType BICGSTAB        */
+                                     (reliable_bicgstab.cc:93-277), QUDA SolverType BICGSTAB.  The
+                                     MdagM systems run the inner CGNE; a BiCGStab breakdown switches
+                                     the rest of the solve to it                                    */
 /* linear systems */
 #define GBC_SYS_MEO 0    /* M~ psi_o = chi_o           (LinOpSystemSolver, syssolver_linop.h)          */
 #define GBC_SYS_MDAGM 1  /* M~^dag M~ psi_o = chi_o    (MdagMSystemSolver, syssolver_mdagm.h:25-35)    */
