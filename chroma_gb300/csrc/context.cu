@@ -1,7 +1,9 @@
 // C-ABI lifecycle, field import and operator application (include/gbclover.h).
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "ctx.h"
 
@@ -160,7 +162,63 @@ void free_ctx_memory(gbc_ctx* c) {
 // shape (one warm-up and three timed launches, CUDA events on the context stream; the launches are
 // idempotent, out never aliases in) and keeps the fastest for the life of the context.  The
 // choices are listed in gbc_last_error-style text by gbc_tune_report; GBC_AUTOTUNE=0 switches it
-// off and uses a fixed shape.
+// off and uses a fixed shape; GBC_TUNE_CACHE keeps the choices across contexts and processes.
+// Persistent tuning (GBC_TUNE_CACHE=<file>, QUDA's tunecache): each decision is appended to the
+// file as "<key> tx nrb minb pair", the key holding the device, lattice, precision, reconstruction,
+// epilogue, isign, reduction, nrhs and a hash of the compiled shape table; later contexts and
+// processes that find their key take the shape without timing.  The file is read once per process
+// (again if the variable changes).
+namespace {
+struct TuneCache {
+  std::mutex m;
+  std::string path;  // file the entries were read from
+  std::map<std::string, std::array<int, 4>> entries;
+};
+TuneCache& tune_cache() {
+  static TuneCache tc;
+  return tc;
+}
+unsigned shape_table_hash() {
+  unsigned h = 2166136261u;  // FNV-1a over the shape tuples
+  for (int i = 0; i < kNumHopShapes; ++i)
+    for (int v : {kHopShapes[i].tx, kHopShapes[i].nrb, kHopShapes[i].minb, kHopShapes[i].pair}) {
+      h ^= (unsigned)v;
+      h *= 16777619u;
+    }
+  return h;
+}
+std::string tune_key(gbc_ctx* c, int prec, int recon, int mode, bool dag, int reduce, int nrhs) {
+  if (c->dev_tag.empty()) {
+    int dev = 0;
+    cudaDeviceProp pr;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&pr, dev) == cudaSuccess) {
+      std::string name = pr.name;
+      for (char& ch : name)
+        if (ch == ' ' || ch == '|') ch = '_';
+      c->dev_tag = name + "|cc" + std::to_string(pr.major) + std::to_string(pr.minor);
+    } else {
+      c->dev_tag = "unknown";
+    }
+  }
+  char buf[384];
+  snprintf(buf, sizeof buf, "%s|%dx%dx%dx%d|prec=%d|recon=%d|mode=%d|dag=%d|reduce=%d|nrhs=%d|shapes=%08x",
+           c->dev_tag.c_str(), c->g.L[0], c->g.L[1], c->g.L[2], c->g.L[3], prec, recon, mode, dag ? 1 : 0, reduce,
+           nrhs, shape_table_hash());
+  return buf;
+}
+void read_tune_cache(TuneCache& tc, const char* path) {
+  tc.entries.clear();
+  tc.path = path;
+  FILE* f = fopen(path, "r");
+  if (!f) return;
+  char line[512], key[400];
+  int tx, nrb, minb, pair;
+  while (fgets(line, sizeof line, f))
+    if (sscanf(line, "%399s %d %d %d %d", key, &tx, &nrb, &minb, &pair) == 5) tc.entries[key] = {tx, nrb, minb, pair};
+  fclose(f);
+}
+}  // namespace
+
 static int default_shape(int nrhs) {
   if (nrhs >= 12 && nrhs % 12 == 0) return 5;
   if (nrhs >= 4) return 3;
@@ -180,6 +238,31 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, int reduce,
     if (si >= 0 && si < kNumHopShapes && hop_shape_valid(kHopShapes[si], prec, h.nrhs, h.g.L[3])) {
       c->tuned[key] = si;
       return si;
+    }
+  }
+  const char* cpath = getenv("GBC_TUNE_CACHE");
+  const bool cached = c->autotune && cpath && *cpath;
+  std::string ckey;
+  if (cached) {
+    ckey = tune_key(c, prec, recon, mode, dag, reduce, h.nrhs);
+    TuneCache& tc = tune_cache();
+    std::lock_guard<std::mutex> lk(tc.m);
+    if (tc.path != cpath) read_tune_cache(tc, cpath);
+    auto e = tc.entries.find(ckey);
+    if (e != tc.entries.end()) {
+      const std::array<int, 4>& t = e->second;
+      for (int si = 0; si < kNumHopShapes; ++si) {
+        const HopShape& sh = kHopShapes[si];
+        if (sh.tx == t[0] && sh.nrb == t[1] && sh.minb == t[2] && sh.pair == t[3] &&
+            hop_shape_valid(sh, prec, h.nrhs, h.g.L[3]) && hop_blocks(sh, h.g.Vh) <= h.part_stride) {
+          char line[160];
+          snprintf(line, sizeof line, "prec=%d mode=%d dag=%d reduce=%d nrhs=%d -> tx=%d nrb=%d minb=%d pair=%d (cache)\n",
+                   prec, mode, dag ? 1 : 0, reduce, h.nrhs, sh.tx, sh.nrb, sh.minb, sh.pair);
+          c->tune_log += line;
+          c->tuned[key] = si;
+          return si;
+        }
+      }
     }
   }
   if (c->autotune) {
@@ -214,6 +297,16 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, int reduce,
              prec, mode, dag ? 1 : 0, reduce, h.nrhs, kHopShapes[best].tx, kHopShapes[best].nrb,
              kHopShapes[best].minb, kHopShapes[best].pair, best_ms / 3 * 1e3);
     c->tune_log += line;
+    if (cached) {
+      const HopShape& sh = kHopShapes[best];
+      TuneCache& tc = tune_cache();
+      std::lock_guard<std::mutex> lk(tc.m);
+      tc.entries[ckey] = {sh.tx, sh.nrb, sh.minb, sh.pair};
+      if (FILE* f = fopen(cpath, "a")) {
+        fprintf(f, "%s %d %d %d %d\n", ckey.c_str(), sh.tx, sh.nrb, sh.minb, sh.pair);
+        fclose(f);
+      }
+    }
   }
   c->tuned[key] = best;
   return best;

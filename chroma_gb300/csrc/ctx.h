@@ -93,6 +93,7 @@ struct gbc_ctx {
   bool autotune = true;
   bool use_graphs = true;  // CUDA-graph replay of CG iteration blocks (GBC_GRAPHS=0: off)
   std::string tune_log;
+  std::string dev_tag;  // device name and compute capability, for the persistent tune cache
 
   // learned preconditioner (opaque, owned by precond.cu)
   void* precond = nullptr;
