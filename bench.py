@@ -172,6 +172,12 @@ def workload(dims):
     return links, src
 
 
+def workload_desc(dims):
+    """The workload string of the JSON line's config (the same for both arms)."""
+    return (f"{'x'.join(map(str, dims))} Wilson-clover propagator, 12 point sources, kappa={KAPPA}, c_sw={CSW}, "
+            f"hot start eps={EPS}, antiperiodic t, full system, FP64 true residual {RSD}")
+
+
 def peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
@@ -311,8 +317,9 @@ def run_reference(args, rank, world):
     line = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * k * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{'x'.join(map(str, dims))} clover propagator, 12 point sources, kappa={KAPPA}, "
-                                   f"c_sw={CSW}, FP64 CGNE (InvCG2) on the host cores"},
+            "config": {"workload": workload_desc(dims),
+                       "solver": "Chroma's FP64 CGNE (InvCG2, CG_INVERTER) restated by the oracle, OpenMP on "
+                                 "the host cores; sources one by one"},
             "cpu_baseline": {"value": value, "unit": "s", "cores": O.load().orc_num_threads(), "kind": "port",
                              "sample": f"{k} InvCG2 iterations per step on 1 source, extrapolated x {iters_full} "
                                        f"iterations x 12 sources"},
@@ -477,9 +484,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f16-storage/f32-arith inner, f64 outer", "data": "synthetic",
-        "config": {"workload": f"{'x'.join(map(str, dims))} Wilson-clover propagator, 12 point sources, "
-                               f"kappa={KAPPA}, c_sw={CSW}, hot start eps={EPS}, antiperiodic t, full system, "
-                               f"FP64 true residual {RSD}",
+        "config": {"workload": workload_desc(dims),
                    "solver": "FP64 defect correction + reliable-update BiCGStab on M~ (FP16 stencil, "
                              f"12-real links, Delta {DELTA}, InnerTol {INNER_TOL}), 12-RHS batch",
                    "l2": "256 MiB L2 flush between timed steps; the fields exceed L2",
