@@ -400,15 +400,19 @@ InnerStats bicgstab(gbc_ctx* c, int pa, int po, double tol, int maxit, double de
   {
     GBC_CUDA(cudaMemcpyAsync(d_sc, hs.data(), sizeof(BiScal) * n, cudaMemcpyHostToDevice, st));
     // the stencil launches of this solve skip right-hand sides whose device flag says converged;
-    // the flags are unset again however the solve ends
+    // the flags are unset, and the iteration graph released, however the solve ends
     static_assert(sizeof(BiScal) % sizeof(int) == 0, "flag stride in ints");
-    struct ActiveScope {
+    cudaGraphExec_t exec = nullptr;
+    struct SolveScope {
       gbc_ctx* c;
-      ~ActiveScope() {
+      cudaGraphExec_t& exec;
+      ~SolveScope() {
         c->hop_active = nullptr;
         c->hop_active_stride = 0;
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
       }
-    } active_scope{c};
+    } solve_scope{c, exec};
     c->hop_active = &d_sc[0].active;
     c->hop_active_stride = (int)(sizeof(BiScal) / sizeof(int));
     auto body = [&]() {
@@ -417,7 +421,6 @@ InnerStats bicgstab(gbc_ctx* c, int pa, int po, double tol, int maxit, double de
       else iteration<PrecS, PrecH>(c, po, d_sc, n, x, r, r0, p, v, s, t, te);
     };
     constexpr int kBlock = 4;
-    cudaGraphExec_t exec = nullptr;
     long long graph_launches = 0;
     int k = 0;
     while (any && k < maxit) {
@@ -492,7 +495,6 @@ InnerStats bicgstab(gbc_ctx* c, int pa, int po, double tol, int maxit, double de
         ++out.reliable;
       }
     }
-    if (exec) cudaGraphExecDestroy(exec);
     GBC_CUDA(cudaMemcpyAsync(hs.data(), d_sc, sizeof(BiScal) * n, cudaMemcpyDeviceToHost, st));
     sync(c);
   }
