@@ -838,6 +838,124 @@ static SolveResult invbicgstab(const Op<double>& M, const cd* chi, cd* psi, doub
   return res;
 }
 
+// RelInvBiCGStab_a (lib/actions/ferm/invert/reliable_bicgstab.cc:18-277): BiCGStab on M with the
+// iterated vectors (r, r0, x, p, v, t) and the operator in single precision, inner products summed
+// in double, and reliable updates in double: whenever |r| fell below Delta times its largest value
+// since the last update, r = b - M x_dble; when it fell below Delta |r| at the last x update, x
+// is also folded into psi and the system restarted from the new residual (b = r_dble, x = 0).
+static SolveResult rel_bicgstab(const Op<double>& A, const Op<float>& AF, const cd* chi, cd* psi, double rsd,
+                                double Delta, int maxit) {
+  const Geom& g = *A.g;
+  const long N = g.V * NSP;
+  const auto& odd = g.sites[1];
+  using cf = std::complex<float>;
+  std::vector<cd> b(N), tmp(N), r_dble(N), x_dble(N);
+  std::vector<cf> r(N), r0(N), x(N), p(N), v(N), t(N);
+  auto dot = [&](const std::vector<cf>& a, const std::vector<cf>& c) {  // <a|c> on rb[1], double sums
+    double re = 0, im = 0;
+#pragma omp parallel for reduction(+ : re, im) schedule(static)
+    for (long i = 0; i < (long)odd.size(); ++i)
+      for (int k = 0; k < NSP; ++k) {
+        const long q = odd[i] * NSP + k;
+        const cd u = std::conj(cd(a[q])) * cd(c[q]);
+        re += u.real();
+        im += u.imag();
+      }
+    return cd(re, im);
+  };
+  SolveResult res{maxit, 0, 0};
+  const double rsd_sq = rsd * rsd * norm2_cb(g, chi, 1);
+  eo_op(A, tmp.data(), psi, +1);
+  for (long s : odd)
+    for (int k = 0; k < NSP; ++k) {
+      const long q = s * NSP + k;
+      b[q] = chi[q] - tmp[q];
+      r[q] = r0[q] = cf((float)b[q].real(), (float)b[q].imag());
+    }
+  double r_sq = norm2_cb(g, b.data(), 1);
+  double rNorm = std::sqrt(r_sq), r0Norm = rNorm, maxrx = rNorm, maxrr = rNorm;
+  cd rho = r_sq, rho_prev = 1.0, alpha = 1.0, omega = 1.0;
+  int k;
+  for (k = 0; k < maxit; ++k) {
+    if (k == 0) {
+      p = r;
+    } else {
+      const cf beta((rho / rho_prev) * (alpha / omega)), om(omega);
+      for (long s : odd)
+        for (int q = 0; q < NSP; ++q) {
+          const long i = s * NSP + q;
+          p[i] = r[i] + beta * (p[i] - om * v[i]);
+        }
+    }
+    eo_op(AF, v.data(), p.data(), +1);
+    const cd r0v = dot(r0, v);
+    if (r0v == cd(0.0)) {
+      res.n_count = -1;  // breakdown: Chroma aborts (reliable_bicgstab.cc:146-149)
+      break;
+    }
+    alpha = rho / r0v;
+    rho_prev = rho;
+    const cf al(alpha);
+    for (long s : odd)
+      for (int q = 0; q < NSP; ++q) r[s * NSP + q] -= al * v[s * NSP + q];  // r now holds s
+    eo_op(AF, t.data(), r.data(), +1);
+    double t_norm = 0;
+    for (long s : odd)
+      for (int q = 0; q < NSP; ++q) t_norm += (double)std::norm(t[s * NSP + q]);
+    omega = dot(t, r) / t_norm;
+    const cf om(omega);
+    for (long s : odd)
+      for (int q = 0; q < NSP; ++q) {
+        const long i = s * NSP + q;
+        x[i] += om * r[i] + al * p[i];
+        r[i] -= om * t[i];
+      }
+    r_sq = 0;
+    for (long s : odd)
+      for (int q = 0; q < NSP; ++q) r_sq += (double)std::norm(r[s * NSP + q]);
+    rho = dot(r0, r);
+    rNorm = std::sqrt(r_sq);
+    maxrx = std::max(maxrx, rNorm);
+    maxrr = std::max(maxrr, rNorm);
+    const bool updateX = rNorm < Delta * r0Norm && r0Norm <= maxrx;
+    const bool updateR = (rNorm < Delta * maxrr && r0Norm <= maxrr) || updateX;
+    if (updateR) {
+      for (long s : odd)
+        for (int q = 0; q < NSP; ++q) x_dble[s * NSP + q] = cd(x[s * NSP + q]);
+      eo_op(A, tmp.data(), x_dble.data(), +1);
+      for (long s : odd)
+        for (int q = 0; q < NSP; ++q) {
+          const long i = s * NSP + q;
+          r_dble[i] = b[i] - tmp[i];
+          r[i] = cf((float)r_dble[i].real(), (float)r_dble[i].imag());
+        }
+      r_sq = norm2_cb(g, r_dble.data(), 1);
+      rNorm = std::sqrt(r_sq);
+      maxrr = rNorm;
+      if (updateX) {
+        for (long s : odd)
+          for (int q = 0; q < NSP; ++q) {
+            const long i = s * NSP + q;
+            psi[i] += x_dble[i];
+            x[i] = 0;
+            b[i] = r_dble[i];
+          }
+        r0Norm = rNorm;
+        maxrx = rNorm;
+      }
+    }
+    if (r_sq < rsd_sq) {
+      for (long s : odd)
+        for (int q = 0; q < NSP; ++q) psi[s * NSP + q] += cd(x[s * NSP + q]);
+      res.n_count = k;  // the loop index at convergence, as the reference reports it (:264)
+      break;
+    }
+  }
+  res.resid = true_resid_linop(A, chi, psi);
+  res.rel_resid = res.resid / std::sqrt(norm2_cb(g, chi, 1));
+  return res;
+}
+
 // FGMRES (NDefl = 0) following lib/actions/ferm/invert/syssolver_linop_fgmres_dr.{h:31-148,
 // cc:77-195, 256-273, 459-765}.  The preconditioner is a callback on full-lattice arrays.
 // ---------------------------------------------------------------------------------------------
@@ -1185,7 +1303,8 @@ void orc_inner_cb(orc_ctx* c, const double* x, const double* y, int cb, double* 
 }
 
 // solver: 0 = CG (LinOpSysSolverCG), 1 = reliable CG (LinOpSysSolverReliableCGClover), 2 = FGMRES,
-// 3 = BiCGStab (LinOpSysSolverBiCGStab, syssolver_linop_bicgstab.h:57-75)
+// 3 = BiCGStab (LinOpSysSolverBiCGStab, syssolver_linop_bicgstab.h:57-75), 4 = reliable mixed
+// BiCGStab (LinOpSysSolverReliableBiCGStabClover, syssolver_linop_rel_bicgstab_clover.h)
 // res[0] = n_count, res[1] = resid, res[2] = rel resid
 int orc_solve(orc_ctx* c, int solver, double* psi, const double* chi, double rsd, int maxit, double delta,
               int nkrylov, precond_fn prec, void* user, double* res) {
@@ -1206,6 +1325,8 @@ int orc_solve(orc_ctx* c, int solver, double* psi, const double* chi, double rsd
     r = fgmres(*c->op, b, x, rsd, nkrylov, maxit, prec, user);
   } else if (solver == 3) {
     r = invbicgstab(*c->op, b, x, rsd, maxit);
+  } else if (solver == 4) {
+    r = rel_bicgstab(*c->op, *c->opf, b, x, rsd, delta, maxit);
   } else {
     return -1;
   }

@@ -16,7 +16,7 @@ _lib = None
 PRECOND_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_void_p)
 
 OP_DSLASH, OP_CLOVER, OP_CLOVER_INV, OP_MEO, OP_MDAGM, OP_UNPREC, OP_SYM, OP_SYM_MDAGM = range(8)
-SOLVER_CG, SOLVER_RELIABLE_CG, SOLVER_FGMRES, SOLVER_BICGSTAB = range(4)
+SOLVER_CG, SOLVER_RELIABLE_CG, SOLVER_FGMRES, SOLVER_BICGSTAB, SOLVER_RELIABLE_BICGSTAB = range(5)
 
 
 def load():

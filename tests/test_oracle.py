@@ -281,6 +281,19 @@ def test_solvers_converge(orc, solver):
     assert true_rel < 5e-9
 
 
+def test_reliable_bicgstab_reaches_fp64_target(orc):
+    # the mixed single/double reliable BiCGStab (the pattern of the GPU inner solver) reaches a
+    # 1e-10 FP64 true residual and the CG solution
+    dims = (4, 4, 4, 8)
+    u = orc.apply_bc(dims, orc.gauge_hot(dims, 0.3, 53), (1, 1, 1, -1))
+    op = OracleOp(dims, u, 1 / (2 * 0.12) - 4, 1.2)
+    chi = rand_spinor(dims, 10, cb=1)
+    x_cg, _ = op.solve(chi, solver=O.SOLVER_CG, rsd=1e-12, maxit=5000)
+    x_rb, r_rb = op.solve(chi, solver=O.SOLVER_RELIABLE_BICGSTAB, rsd=1e-10, maxit=5000, delta=0.1)
+    assert r_rb["n_count"] > 0 and r_rb["rel_resid"] <= 1.05e-10, r_rb
+    assert np.linalg.norm(x_rb - x_cg) < 1e-8 * np.linalg.norm(x_cg)
+
+
 def test_bicgstab_matches_cg(orc):
     # BiCGStab on M~ (no normal equations) and CGNE reach the same solution, BiCGStab in fewer
     # operator applications (2 per iteration for both)
