@@ -12,6 +12,10 @@
 //                           refreshed from an FP32 operator (reliable updates)
 //   GBC_SOLVER_FGMRES       FGMRES(NKrylov), NDefl = 0 (fgmres below), optionally preconditioned by
 //                           the learned network (precond.cu), inside the same FP64 defect correction
+//   GBC_SOLVER_BICGSTAB     the same FP64 defect correction around a reliable BiCGStab on M~
+//                           (bicgstab.cu; RELIABLE_BICGSTAB_MP_CLOVER_INVERTER, reliable_bicgstab.cc:
+//                           18-277); MdagM systems, and the rest of a solve whose inner BiCGStab broke
+//                           down or raised the residual, use the inner CGNE
 //
 // Every right-hand side carries its own scalars on the device (CGScalars); a converged right-hand
 // side keeps alpha = beta = 0 so that the batch can run on until the last one converges.
