@@ -1,6 +1,7 @@
-// BLAS-1 on checkerboard spinor fields (any storage precision per operand), with FP64
-// accumulation of every reduction: per-block partial sums in a fixed grid, then one
-// deterministic finalize pass.  Also the device-side CG scalar logic, so that an iteration
+// BLAS-1 on checkerboard spinor fields (any storage precision per operand).  Reductions sum a
+// thread's sites and a warp's lanes in the operands' compute precision (FP32 unless an operand is
+// FP64: GB300's FP64 pipe made per-site FP64 sums the bottleneck of bandwidth-bound kernels), then
+// per-warp and per-block sums in FP64 in a fixed grid, then one deterministic finalize pass.  Also the device-side CG scalar logic, so that an iteration
 // needs no host round trip (InvCG2, lib/actions/ferm/invert/invcg2.cc:153-221).
 #include "gbc_device.cuh"
 
