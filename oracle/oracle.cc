@@ -956,6 +956,95 @@ static SolveResult rel_bicgstab(const Op<double>& A, const Op<float>& AF, const 
   return res;
 }
 
+// InvMultiPrecRichardson (lib/actions/ferm/invert/inv_multiprec_richardson.cc:13-107): the FP64
+// defect correction r = b - A x; repeat { dx = Dinv r in single precision; x += dx; r -= A dx in
+// double } until |r|^2 <= RsdTarget^2 |b|^2, then the true residual.  Dinv here is a plain
+// single-precision BiCGStab on A (the InvBiCGStab recursion of invbicgstab.cc:12-200 on float
+// fields, inner products summed in double) to relative tolerance inner_tol.  n_count = total inner
+// iterations; the outer step count goes to *outer.
+static SolveResult richardson_bicgstab(const Op<double>& A, const Op<float>& AF, const cd* chi, cd* psi, double rsd,
+                                       double inner_tol, int maxit, int* outer) {
+  const Geom& g = *A.g;
+  const long N = g.V * NSP;
+  const auto& odd = g.sites[1];
+  using cf = std::complex<float>;
+  std::vector<cd> r(N), tmp(N), dx(N);
+  std::vector<cf> rr(N), rr0(N), e(N), p(N), v(N), t(N);
+  auto dot = [&](const std::vector<cf>& a, const std::vector<cf>& c) {
+    double re = 0, im = 0;
+#pragma omp parallel for reduction(+ : re, im) schedule(static)
+    for (long i = 0; i < (long)odd.size(); ++i)
+      for (int k = 0; k < NSP; ++k) {
+        const long q = odd[i] * NSP + k;
+        const cd u = std::conj(cd(a[q])) * cd(c[q]);
+        re += u.real();
+        im += u.imag();
+      }
+    return cd(re, im);
+  };
+  SolveResult res{0, 0, 0};
+  const double rsd_t = rsd * rsd * norm2_cb(g, chi, 1);
+  eo_op(A, tmp.data(), psi, +1);
+  for (long s : odd)
+    for (int k = 0; k < NSP; ++k) r[s * NSP + k] = chi[s * NSP + k] - tmp[s * NSP + k];
+  double rnorm = norm2_cb(g, r.data(), 1);
+  int steps = 0;
+  while (rnorm > rsd_t && steps < 100 && res.n_count < maxit) {
+    ++steps;
+    // Dinv: single-precision BiCGStab on A e = r from e = 0
+    for (long s : odd)
+      for (int k = 0; k < NSP; ++k) {
+        const long q = s * NSP + k;
+        rr[q] = rr0[q] = cf((float)r[q].real(), (float)r[q].imag());
+        e[q] = p[q] = v[q] = 0;
+      }
+    const double in_sq = inner_tol * inner_tol * dot(rr, rr).real();
+    cd rho_prev = 1.0, alpha = 1.0, omega = 1.0;
+    for (int k = 1; k <= maxit - res.n_count; ++k) {
+      const cd rho = dot(rr0, rr);
+      if (rho == cd(0.0)) break;
+      const cf beta((rho / rho_prev) * (alpha / omega)), om0(omega);
+      for (long s : odd)
+        for (int q = 0; q < NSP; ++q) {
+          const long i = s * NSP + q;
+          p[i] = rr[i] + beta * (p[i] - om0 * v[i]);
+        }
+      eo_op(AF, v.data(), p.data(), +1);
+      alpha = rho / dot(rr0, v);
+      rho_prev = rho;
+      const cf al(alpha);
+      for (long s : odd)
+        for (int q = 0; q < NSP; ++q) rr[s * NSP + q] -= al * v[s * NSP + q];
+      eo_op(AF, t.data(), rr.data(), +1);
+      omega = dot(t, rr) / dot(t, t).real();
+      const cf om(omega);
+      for (long s : odd)
+        for (int q = 0; q < NSP; ++q) {
+          const long i = s * NSP + q;
+          e[i] += om * rr[i] + al * p[i];
+          rr[i] -= om * t[i];
+        }
+      ++res.n_count;
+      if (dot(rr, rr).real() < in_sq) break;
+    }
+    // x += dx; r -= A dx in double
+    for (long s : odd)
+      for (int k = 0; k < NSP; ++k) dx[s * NSP + k] = cd(e[s * NSP + k]);
+    eo_op(A, tmp.data(), dx.data(), +1);
+    for (long s : odd)
+      for (int k = 0; k < NSP; ++k) {
+        const long q = s * NSP + k;
+        psi[q] += dx[q];
+        r[q] -= tmp[q];
+      }
+    rnorm = norm2_cb(g, r.data(), 1);
+  }
+  if (outer) *outer = steps;
+  res.resid = true_resid_linop(A, chi, psi);
+  res.rel_resid = res.resid / std::sqrt(norm2_cb(g, chi, 1));
+  return res;
+}
+
 // FGMRES (NDefl = 0) following lib/actions/ferm/invert/syssolver_linop_fgmres_dr.{h:31-148,
 // cc:77-195, 256-273, 459-765}.  The preconditioner is a callback on full-lattice arrays.
 // ---------------------------------------------------------------------------------------------
@@ -1304,7 +1393,9 @@ void orc_inner_cb(orc_ctx* c, const double* x, const double* y, int cb, double* 
 
 // solver: 0 = CG (LinOpSysSolverCG), 1 = reliable CG (LinOpSysSolverReliableCGClover), 2 = FGMRES,
 // 3 = BiCGStab (LinOpSysSolverBiCGStab, syssolver_linop_bicgstab.h:57-75), 4 = reliable mixed
-// BiCGStab (LinOpSysSolverReliableBiCGStabClover, syssolver_linop_rel_bicgstab_clover.h)
+// BiCGStab (LinOpSysSolverReliableBiCGStabClover, syssolver_linop_rel_bicgstab_clover.h),
+// 5 = multi-precision Richardson around a single-precision BiCGStab (inner tolerance = delta);
+// res[3] = outer steps (solver 5)
 // res[0] = n_count, res[1] = resid, res[2] = rel resid
 int orc_solve(orc_ctx* c, int solver, double* psi, const double* chi, double rsd, int maxit, double delta,
               int nkrylov, precond_fn prec, void* user, double* res) {
@@ -1327,6 +1418,10 @@ int orc_solve(orc_ctx* c, int solver, double* psi, const double* chi, double rsd
     r = invbicgstab(*c->op, b, x, rsd, maxit);
   } else if (solver == 4) {
     r = rel_bicgstab(*c->op, *c->opf, b, x, rsd, delta, maxit);
+  } else if (solver == 5) {
+    int outer = 0;
+    r = richardson_bicgstab(*c->op, *c->opf, b, x, rsd, delta, maxit, &outer);
+    res[3] = outer;
   } else {
     return -1;
   }

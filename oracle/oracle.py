@@ -16,7 +16,8 @@ _lib = None
 PRECOND_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_void_p)
 
 OP_DSLASH, OP_CLOVER, OP_CLOVER_INV, OP_MEO, OP_MDAGM, OP_UNPREC, OP_SYM, OP_SYM_MDAGM = range(8)
-SOLVER_CG, SOLVER_RELIABLE_CG, SOLVER_FGMRES, SOLVER_BICGSTAB, SOLVER_RELIABLE_BICGSTAB = range(5)
+(SOLVER_CG, SOLVER_RELIABLE_CG, SOLVER_FGMRES, SOLVER_BICGSTAB, SOLVER_RELIABLE_BICGSTAB,
+ SOLVER_RICHARDSON_BICGSTAB) = range(6)
 
 
 def load():
@@ -230,7 +231,7 @@ class OracleOp:
               precond=None):
         chi = self._vec(chi)
         psi = np.zeros_like(chi) if psi0 is None else self._vec(psi0).copy()
-        res = np.zeros(3)
+        res = np.zeros(4)  # n_count, resid, rel_resid, outer steps (multi-precision Richardson)
         V = self.V
         if precond is not None:
             def _cb(user, out, inp):
@@ -242,7 +243,8 @@ class OracleOp:
             cbf = PRECOND_FN()
         self.lib.orc_solve(self.h, int(solver), _dp(psi.view(np.float64)), _dp(chi.view(np.float64)),
                            float(rsd), int(maxit), float(delta), int(nkrylov), cbf, None, _dp(res))
-        return psi, {"n_count": int(res[0]), "resid": float(res[1]), "rel_resid": float(res[2])}
+        return psi, {"n_count": int(res[0]), "resid": float(res[1]), "rel_resid": float(res[2]),
+                     "n_outer": int(res[3])}
 
     def qprop(self, chi, rsd=1e-10, maxit=10000):
         chi = self._vec(chi)

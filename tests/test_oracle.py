@@ -294,6 +294,20 @@ def test_reliable_bicgstab_reaches_fp64_target(orc):
     assert np.linalg.norm(x_rb - x_cg) < 1e-8 * np.linalg.norm(x_cg)
 
 
+def test_richardson_multiprec_defect_correction(orc):
+    # InvMultiPrecRichardson with a single-precision BiCGStab inner solve to 1e-5 (the outer pattern
+    # of the GPU mixed solvers): FP64 true residual 1e-10 in a few outer steps, the CG solution
+    dims = (4, 4, 4, 8)
+    u = orc.apply_bc(dims, orc.gauge_hot(dims, 0.3, 54), (1, 1, 1, -1))
+    op = OracleOp(dims, u, 1 / (2 * 0.12) - 4, 1.2)
+    chi = rand_spinor(dims, 11, cb=1)
+    x_cg, _ = op.solve(chi, solver=O.SOLVER_CG, rsd=1e-12, maxit=5000)
+    x_rm, r_rm = op.solve(chi, solver=O.SOLVER_RICHARDSON_BICGSTAB, rsd=1e-10, maxit=5000, delta=1e-5)
+    assert r_rm["rel_resid"] <= 1.05e-10, r_rm
+    assert 2 <= r_rm["n_outer"] <= 4, r_rm
+    assert np.linalg.norm(x_rm - x_cg) < 1e-8 * np.linalg.norm(x_cg)
+
+
 def test_bicgstab_matches_cg(orc):
     # BiCGStab on M~ (no normal equations) and CGNE reach the same solution, BiCGStab in fewer
     # operator applications (2 per iteration for both)
