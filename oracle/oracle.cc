@@ -1075,6 +1075,65 @@ struct Givens {
   }
 };
 
+// Backward substitution R eta = g on the first n_cols rows of the upper-triangular R
+// (LeastSquaresSolve, syssolver_linop_fgmres_dr.cc:256-273); R[col][row] as H.
+static void least_squares(const std::vector<std::vector<cd>>& R, const std::vector<cd>& gvec, std::vector<cd>& eta,
+                          int n_cols) {
+  eta[n_cols - 1] = gvec[n_cols - 1] / R[n_cols - 1][n_cols - 1];
+  for (int row = n_cols - 2; row >= 0; --row) {
+    eta[row] = gvec[row];
+    for (int col = row + 1; col < n_cols; ++col) eta[row] -= R[col][row] * eta[col];
+    eta[row] /= R[row][row];
+  }
+}
+
+// The matrices of one Arnoldi cycle: H[j][i] is column j, row i (Chroma's H(j,i)); R is H with the
+// cycle's Givens rotations applied (upper triangular); g the rotated right-hand side |r| e_0.
+struct ArnoldiCycle {
+  std::vector<std::vector<cd>> H, R;
+  std::vector<cd> g;
+  std::vector<Givens> rots;
+  explicit ArnoldiCycle(int nk) : H(nk, std::vector<cd>(nk + 1, 0.0)), R(H), g(nk + 1, 0.0) {}
+};
+
+// One flexible Arnoldi cycle without deflation (FlexibleArnoldiT, syssolver_linop_fgmres_dr.cc:78-195):
+// z_j = M v_j, w = A z_j, one modified Gram-Schmidt pass of w against v_0..v_j into column j of H,
+// v_{j+1} = w / |w|, column j of R = H's column with the earlier rotations applied, then a new rotation
+// that zeroes R(j, j+1), applied to g too.  The cycle ends when |g_{j+1}| <= target (the accumulated
+// residual norm), at a happy breakdown (|w| < 1e-14: dimension j), after nkrylov columns or when
+// iters reaches maxit.  V[0] and cy.g[0] are set by the caller.  Returns the cycle's dimension.
+static int flexible_arnoldi(const Op<double>& A, int nkrylov, double target, int maxit, int& iters,
+                            precond_fn prec, void* user, std::vector<std::vector<cd>>& V,
+                            std::vector<std::vector<cd>>& Z, std::vector<cd>& w, ArnoldiCycle& cy) {
+  const Geom& g = *A.g;
+  const auto& odd = g.sites[1];
+  auto& H = cy.H;
+  auto& R = cy.R;
+  int dim = 0;
+  for (int j = 0; j < nkrylov && iters < maxit; ++j) {
+    if (prec) prec(user, Z[j].data(), V[j].data());
+    else for (long s : odd) for (int k = 0; k < NSP; ++k) Z[j][s * NSP + k] = V[j][s * NSP + k];
+    eo_op(A, w.data(), Z[j].data(), +1);
+    for (int i = 0; i <= j; ++i) {
+      H[j][i] = inner_cb(g, V[i].data(), w.data(), 1);
+      axpby_cb<double, cd>(g, -H[j][i], V[i].data(), 1.0, w.data(), 1);
+    }
+    double wnorm = std::sqrt(norm2_cb(g, w.data(), 1));
+    H[j][j + 1] = wnorm;
+    ++iters;
+    if (std::fabs(wnorm) < 1e-14) return j;  // happy breakdown (cc:118-127)
+    for (long s : odd) for (int k = 0; k < NSP; ++k) V[j + 1][s * NSP + k] = w[s * NSP + k] / wnorm;
+    for (int i = 0; i <= j + 1; ++i) R[j][i] = H[j][i];
+    for (int i = 0; i < j; ++i) cy.rots[i].apply_col(j, R);
+    cy.rots.emplace_back(j, R);
+    cy.rots[j].apply_col(j, R);
+    cy.rots[j].apply_vec(cy.g);
+    dim = j + 1;
+    if (std::fabs(cy.g[j + 1].real()) <= target) break;
+  }
+  return dim;
+}
+
 static SolveResult fgmres(const Op<double>& A, const cd* chi, cd* psi, double rsd_target, int nkrylov, int maxit,
                           precond_fn prec, void* user) {
   const Geom& g = *A.g;
@@ -1093,43 +1152,13 @@ static SolveResult fgmres(const Op<double>& A, const cd* chi, cd* psi, double rs
   double r_norm = resid();
   int iters = 0;
   while (r_norm > target && iters < maxit) {
-    // H[j][i]: column j, row i (Chroma's H(j,i))
-    std::vector<std::vector<cd>> H(nkrylov, std::vector<cd>(nkrylov + 1, 0.0)), R = H;
-    std::vector<cd> gvec(nkrylov + 1, 0.0);
-    std::vector<Givens> rots;
-    gvec[0] = r_norm;
+    ArnoldiCycle cy(nkrylov);
+    cy.g[0] = r_norm;
     for (long s : odd) for (int k = 0; k < NSP; ++k) V[0][s * NSP + k] = r[s * NSP + k] / r_norm;
-    int dim = 0;
-    for (int j = 0; j < nkrylov && iters < maxit; ++j) {
-      if (prec) prec(user, Z[j].data(), V[j].data());
-      else for (long s : odd) for (int k = 0; k < NSP; ++k) Z[j][s * NSP + k] = V[j][s * NSP + k];
-      eo_op(A, w.data(), Z[j].data(), +1);
-      for (int i = 0; i <= j; ++i) {
-        H[j][i] = inner_cb(g, V[i].data(), w.data(), 1);
-        axpby_cb<double, cd>(g, -H[j][i], V[i].data(), 1.0, w.data(), 1);
-      }
-      double wnorm = std::sqrt(norm2_cb(g, w.data(), 1));
-      H[j][j + 1] = wnorm;
-      ++iters;
-      if (std::fabs(wnorm) < 1e-14) { dim = j; break; }  // happy breakdown (cc:123-131)
-      for (long s : odd) for (int k = 0; k < NSP; ++k) V[j + 1][s * NSP + k] = w[s * NSP + k] / wnorm;
-      for (int i = 0; i <= j + 1; ++i) R[j][i] = H[j][i];
-      for (int i = 0; i < j; ++i) rots[i].apply_col(j, R);
-      rots.emplace_back(j, R);
-      rots[j].apply_col(j, R);
-      rots[j].apply_vec(gvec);
-      dim = j + 1;
-      if (std::fabs(gvec[j + 1].real()) <= target) break;
-    }
+    int dim = flexible_arnoldi(A, nkrylov, target, maxit, iters, prec, user, V, Z, w, cy);
     if (dim == 0) break;
-    // least squares (cc:256-273)
     std::vector<cd> eta(dim);
-    eta[dim - 1] = gvec[dim - 1] / R[dim - 1][dim - 1];
-    for (int row = dim - 2; row >= 0; --row) {
-      eta[row] = gvec[row];
-      for (int col = row + 1; col < dim; ++col) eta[row] -= R[col][row] * eta[col];
-      eta[row] /= R[row][row];
-    }
+    least_squares(cy.R, cy.g, eta, dim);
     for (int j = 0; j < dim; ++j) axpby_cb<double, cd>(g, eta[j], Z[j].data(), 1.0, psi, 1);
     r_norm = resid();
   }
@@ -1519,6 +1548,75 @@ int orc_read_nersc(const char* path, int* dims, double* links, long cap_sites, d
       store_m3(&u[(s * 4 + mu) * 9], m);
     }
   return 0;
+}
+
+// Givens rotation of syssolver_linop_fgmres_dr.h:31-148 built on column col of H (rows col, col + 1),
+// applied to each column in cols and then, when vec is not null, to vec (nrows complex): the
+// Givens* fixtures of mainprogs/tests/fgmres_dr_tests.cc:251-375.  H holds ncols columns of nrows
+// complex numbers (Chroma's H(col, row)).  Returns -1 on an index outside H.
+int orc_givens(int ncols, int nrows, double* H, int col, const int* cols, int ncols_apply, double* vec) {
+  if (col < 0 || col >= ncols || col + 1 >= nrows) return -1;
+  for (int k = 0; k < ncols_apply; ++k)
+    if (cols[k] < 0 || cols[k] >= ncols) return -1;
+  cd* h = reinterpret_cast<cd*>(H);
+  std::vector<std::vector<cd>> M(ncols, std::vector<cd>(nrows));
+  for (int j = 0; j < ncols; ++j) for (int i = 0; i < nrows; ++i) M[j][i] = h[(long)j * nrows + i];
+  Givens G(col, M);
+  for (int k = 0; k < ncols_apply; ++k) G.apply_col(cols[k], M);
+  for (int j = 0; j < ncols; ++j) for (int i = 0; i < nrows; ++i) h[(long)j * nrows + i] = M[j][i];
+  if (vec) {
+    cd* v = reinterpret_cast<cd*>(vec);
+    std::vector<cd> t(v, v + nrows);
+    G.apply_vec(t);
+    std::copy(t.begin(), t.end(), v);
+  }
+  return 0;
+}
+
+// Backward substitution R x = b over the first n_cols rows of the upper-triangular R (ncols columns of
+// nrows complex, n_cols <= ncols, n_cols <= nrows): the testLeastSquares fixture of
+// fgmres_dr_tests.cc:527-567.  Returns -1 on bad sizes.
+int orc_least_squares(int ncols, int nrows, const double* R, const double* b, int n_cols, double* x) {
+  if (n_cols < 1 || n_cols > ncols || n_cols > nrows) return -1;
+  const cd* r = reinterpret_cast<const cd*>(R);
+  std::vector<std::vector<cd>> M(ncols, std::vector<cd>(nrows));
+  for (int j = 0; j < ncols; ++j) for (int i = 0; i < nrows; ++i) M[j][i] = r[(long)j * nrows + i];
+  std::vector<cd> bv(reinterpret_cast<const cd*>(b), reinterpret_cast<const cd*>(b) + nrows), eta(n_cols);
+  least_squares(M, bv, eta, n_cols);
+  std::copy(eta.begin(), eta.end(), reinterpret_cast<cd*>(x));
+  return 0;
+}
+
+// One flexible Arnoldi cycle of the even-odd operator with the identity preconditioner from
+// v_0 = chi / |chi|, g = |chi| e_0, stopping at |g_{j+1}| <= rsd_target |chi| (the arnoldi5 and
+// arnoldi5GivensRot fixtures, fgmres_dr_tests.cc:162-249, 377-524).  V: nkrylov + 1 full-lattice
+// spinors (odd sites written, the rest zero); H, R: nkrylov columns of nkrylov + 1 complex rows;
+// g: nkrylov + 1 complex.  Returns the cycle's dimension, -1 on nkrylov < 1.
+int orc_arnoldi(orc_ctx* c, int nkrylov, const double* chi, double rsd_target, double* V_out, double* H_out,
+                double* R_out, double* g_out) {
+  if (nkrylov < 1) return -1;
+  const Geom& g = *c->g;
+  const long N = g.V * NSP;
+  const cd* b = reinterpret_cast<const cd*>(chi);
+  double beta = std::sqrt(norm2_cb(g, b, 1));
+  std::vector<std::vector<cd>> V(nkrylov + 1, std::vector<cd>(N, 0.0)), Z(nkrylov, std::vector<cd>(N, 0.0));
+  std::vector<cd> w(N, 0.0);
+  for (long s : g.sites[1]) for (int k = 0; k < NSP; ++k) V[0][s * NSP + k] = b[s * NSP + k] / beta;
+  ArnoldiCycle cy(nkrylov);
+  cy.g[0] = beta;
+  int iters = 0;
+  int dim = flexible_arnoldi(*c->op, nkrylov, rsd_target * beta, nkrylov, iters, nullptr, nullptr, V, Z, w, cy);
+  cd* vo = reinterpret_cast<cd*>(V_out);
+  for (int j = 0; j <= nkrylov; ++j) std::copy(V[j].begin(), V[j].end(), vo + (long)j * N);
+  cd* ho = reinterpret_cast<cd*>(H_out);
+  cd* ro = reinterpret_cast<cd*>(R_out);
+  for (int j = 0; j < nkrylov; ++j)
+    for (int i = 0; i <= nkrylov; ++i) {
+      ho[(long)j * (nkrylov + 1) + i] = cy.H[j][i];
+      ro[(long)j * (nkrylov + 1) + i] = cy.R[j][i];
+    }
+  std::copy(cy.g.begin(), cy.g.end(), reinterpret_cast<cd*>(g_out));
+  return dim;
 }
 
 }  // extern "C"

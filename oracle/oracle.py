@@ -63,6 +63,9 @@ def load():
     lib.orc_normal.argtypes = [C.c_uint64, C.c_uint64]
     lib.orc_num_threads.restype = C.c_int
     lib.orc_set_threads.argtypes = [C.c_int]
+    lib.orc_givens.argtypes = [C.c_int, C.c_int, dp, C.c_int, ip, C.c_int, dp]
+    lib.orc_least_squares.argtypes = [C.c_int, C.c_int, dp, dp, C.c_int, dp]
+    lib.orc_arnoldi.argtypes = [C.c_void_p, C.c_int, dp, C.c_double, dp, dp, dp, dp]
     _lib = lib
     return lib
 
@@ -75,6 +78,34 @@ def _dp(a):
 def _ip(a):
     a = np.ascontiguousarray(a, dtype=np.int32)
     return a, a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def givens(H, col, cols, vec=None):
+    """Build the FGMRES Givens rotation on column ``col`` of H (complex, shape (ncols, nrows):
+    Chroma's H(col, row)), apply it to the listed columns and to ``vec``; returns the new H, vec."""
+    lib = load()
+    H = np.array(H, dtype=np.complex128, order="C")
+    ncols, nrows = H.shape
+    cols_a, cols_p = _ip(np.asarray(cols, dtype=np.int32).reshape(-1))
+    v = None if vec is None else np.array(vec, dtype=np.complex128).reshape(nrows)
+    rc = lib.orc_givens(ncols, nrows, _dp(H.view(np.float64)), int(col), cols_p, len(cols_a),
+                        None if v is None else _dp(v.view(np.float64)))
+    if rc != 0:
+        raise ValueError("bad Givens column")
+    return H, v
+
+
+def least_squares(R, b, n_cols):
+    """x with R[:n_cols] x = b[:n_cols] for the upper-triangular R of shape (ncols, nrows)."""
+    lib = load()
+    R = np.ascontiguousarray(R, dtype=np.complex128)
+    ncols, nrows = R.shape
+    b = np.ascontiguousarray(b, dtype=np.complex128).reshape(nrows)
+    x = np.zeros(n_cols, dtype=np.complex128)
+    if lib.orc_least_squares(ncols, nrows, _dp(R.view(np.float64)), _dp(b.view(np.float64)), int(n_cols),
+                             _dp(x.view(np.float64))) != 0:
+        raise ValueError("bad least-squares sizes")
+    return x
 
 
 def volume(dims):
@@ -245,6 +276,21 @@ class OracleOp:
                            float(rsd), int(maxit), float(delta), int(nkrylov), cbf, None, _dp(res))
         return psi, {"n_count": int(res[0]), "resid": float(res[1]), "rel_resid": float(res[2]),
                      "n_outer": int(res[3])}
+
+    def arnoldi(self, chi, nkrylov, rsd=1e-6):
+        """One flexible Arnoldi cycle of M~ (identity preconditioner) from chi / |chi|: returns
+        V (nkrylov+1, V, 12), H and R (nkrylov, nkrylov+1; H[col, row]), g (nkrylov+1) and the dimension."""
+        chi = self._vec(chi)
+        nk = int(nkrylov)
+        Vs = np.zeros((nk + 1, self.V, 12), dtype=np.complex128)
+        H = np.zeros((nk, nk + 1), dtype=np.complex128)
+        R = np.zeros_like(H)
+        g = np.zeros(nk + 1, dtype=np.complex128)
+        dim = self.lib.orc_arnoldi(self.h, nk, _dp(chi.view(np.float64)), float(rsd), _dp(Vs.view(np.float64)),
+                                   _dp(H.view(np.float64)), _dp(R.view(np.float64)), _dp(g.view(np.float64)))
+        if dim < 0:
+            raise ValueError("bad Krylov size")
+        return Vs, H, R, g, dim
 
     def qprop(self, chi, rsd=1e-10, maxit=10000):
         chi = self._vec(chi)
