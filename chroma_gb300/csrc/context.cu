@@ -561,8 +561,8 @@ int gbc_load_gauge(gbc_ctx* c, const double* links) {
     sync(c);
     cudaFree(d_logdet);
     cudaFree(d_nneg);
-    // log det and negative pivots of A_ee (Chroma's cholesDet(0))
-    double s = 0;
+    // log det and negative pivots of A_ee (Chroma's cholesDet(0)); log det of A_oo (cholesDet(1))
+    double s = 0, s_odd = 0;
     int n = 0;
     for (long i = 0; i < V; ++i) {
       long r = i;
@@ -571,11 +571,15 @@ int gbc_load_gauge(gbc_ctx* c, const double* links) {
         par += (int)(r % c->dims[k]);
         r /= c->dims[k];
       }
-      if (par & 1) continue;
+      if (par & 1) {
+        s_odd += ld[i];
+        continue;
+      }
       s += ld[i];
       n += nn[i];
     }
     c->logdet_even = s;
+    c->logdet_odd = s_odd;
     c->nneg = n;
     ++c->gauge_version;
     if (n && c->opts.verbose) fprintf(stderr, "gbclover: WARNING %d negative clover eigenvalues\n", n);
@@ -609,6 +613,14 @@ int gbc_get_clover(gbc_ctx* c, double* clov, double* inv, double* logdet, int* n
     if (nneg) *nneg = c->nneg;
     return GBC_OK;
   });
+}
+
+int gbc_get_logdet(gbc_ctx* c, double* logdet_even, double* logdet_odd) {
+  if (!c || (!logdet_even && !logdet_odd)) return GBC_ERR_ARGS;
+  if (!c->have_gauge) return fail(c, GBC_ERR_STATE, "load the gauge field first");
+  if (logdet_even) *logdet_even = c->logdet_even;
+  if (logdet_odd) *logdet_odd = c->logdet_odd;
+  return GBC_OK;
 }
 
 int gbc_apply(gbc_ctx* c, int op, int isign, int cb, int prec, int nrhs, double* out, const double* in) {

@@ -53,7 +53,8 @@ struct gbc_ctx {
   double* d_links = nullptr;  // [V][4][3][3] complex = 72 doubles per site
   double* d_clov = nullptr;   // [V][72]
   double* d_inv = nullptr;    // [V][72] A^-1 (both parities)
-  double logdet_even = 0;
+  double logdet_even = 0;  // sum over even sites of log|d| of A's LDL^dag factors
+  double logdet_odd = 0;   // the same over the odd sites
   int nneg = 0;
 
   gbc::PrecFields pf[3];

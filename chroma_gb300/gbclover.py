@@ -25,7 +25,7 @@ SYS_MEO, SYS_MDAGM, SYS_FULL, SYS_SYM, SYS_SYM_MDAGM = range(5)
 
 # every entry point include/gbclover.h declares
 EXPORTS = ["gbc_create", "gbc_destroy", "gbc_strerror", "gbc_last_error", "gbc_load_gauge", "gbc_load_clover",
-           "gbc_get_clover", "gbc_apply", "gbc_solve", "gbc_solve_device", "gbc_load_precond",
+           "gbc_get_clover", "gbc_get_logdet", "gbc_apply", "gbc_solve", "gbc_solve_device", "gbc_load_precond",
            "gbc_gauge_synthetic", "gbc_time_operator", "gbc_tune_report", "gbc_apply_meo_noalloc",
            "gbc_precond_init", "gbc_precond_save", "gbc_precond_weights", "gbc_precond_set_weights",
            "gbc_precond_apply", "gbc_precond_loss_grad", "gbc_precond_train", "gbc_batch_create",
@@ -88,6 +88,7 @@ def load(path=LIB_PATH):
     lib.gbc_load_gauge.argtypes = [C.c_void_p, dp]
     lib.gbc_load_clover.argtypes = [C.c_void_p, dp, dp]
     lib.gbc_get_clover.argtypes = [C.c_void_p, dp, dp, dp, C.POINTER(C.c_int)]
+    lib.gbc_get_logdet.argtypes = [C.c_void_p, dp, dp]
     lib.gbc_apply.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp]
     lib.gbc_solve.argtypes = [C.c_void_p, C.POINTER(SolveParams), C.c_int, dp, dp, C.POINTER(Result)]
     lib.gbc_solve_device.argtypes = [C.c_void_p, C.POINTER(SolveParams), C.c_int, C.c_void_p, C.c_void_p,
@@ -209,6 +210,13 @@ class Context:
         nn = C.c_int()
         self._check(self.lib.gbc_get_clover(self.h, _dp(a), _dp(b), C.byref(ld), C.byref(nn)), "get_clover")
         return a, b, ld.value, nn.value
+
+    def logdet(self):
+        """(sum_even, sum_odd) of log|d| over the clover blocks' LDL^dag factors."""
+        e = C.c_double()
+        o = C.c_double()
+        self._check(self.lib.gbc_get_logdet(self.h, C.byref(e), C.byref(o)), "get_logdet")
+        return e.value, o.value
 
     def _fields(self, x):
         x = np.ascontiguousarray(x, dtype=np.complex128)

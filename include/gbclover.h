@@ -160,6 +160,11 @@ int gbc_load_clover(gbc_ctx* ctx, const double* clov, const double* invclov_even
 /* Packed A and A^-1 (even sites; odd sites zero) and sum_even log|d| (cholesDet(0),
    clover_term_qdp_w.h:580-606); any output pointer may be NULL. */
 int gbc_get_clover(gbc_ctx* ctx, double* clov, double* invclov, double* logdet_even, int* n_negative);
+/* Log determinants of the clover blocks of the field gbc_load_gauge built: sum_even log|d|
+   (EvenOddPrecCloverLinOp::logDetEvenEvenLinOp, eoprec_clover_linop_w.cc:310-312) and sum_odd
+   log|d| (SymEvenOddPrecCloverLinOp::logDetOddOddLinOp, seoprec_clover_linop_w.cc:490-492);
+   either pointer may be NULL, not both. */
+int gbc_get_logdet(gbc_ctx* ctx, double* logdet_even, double* logdet_odd);
 
 /* ---- operators (parity tests; LinearOperator<LatticeFermion>::operator(), lib/linearop.h:25-49) */
 /* out/in: nrhs host spinors (full lattice); only the parity the operator reads/writes matters;

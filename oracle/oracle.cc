@@ -436,7 +436,8 @@ struct Op {
   std::vector<CloverSite<R>> invclov;  // A^-1 on all sites (the odd ones serve the symmetric operator)
   bool twisted = false;
   R twisted_m = 0;
-  double logdet_even = 0;
+  double logdet_even = 0;   // cholesDet(0)
+  double logdet_odd = 0;    // cholesDet(1), the symmetric operator's logDetOddOddLinOp
   int nneg = 0;
 };
 
@@ -1317,6 +1318,7 @@ orc_ctx* orc_create(const int* dims, const double* links, double mass, double cs
   double ld_odd = 0;
   int nneg_odd = 0;
   for (long s : g.sites[1]) ldl_invert_site(op.invclov[s], ld_odd, nneg_odd);
+  op.logdet_odd = ld_odd;
   op.twisted = twisted != 0;
   op.twisted_m = twisted_m;
   // single-precision copy for the reliable CG inner operator
@@ -1350,6 +1352,8 @@ void orc_destroy(orc_ctx* c) {
 
 long orc_volume(orc_ctx* c) { return c->g->V; }
 double orc_logdet_even(orc_ctx* c) { return c->op->logdet_even; }
+// sum over the odd sites of log|d| of A's LDL^dag factors (seoprec_clover_linop_w.cc:490-492)
+double orc_logdet_odd(orc_ctx* c) { return c->op->logdet_odd; }
 int orc_neg_eigs(orc_ctx* c) { return c->op->nneg; }
 
 // Packed clover (72 doubles/site) of A and of A^-1, all sites.

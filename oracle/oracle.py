@@ -42,6 +42,8 @@ def load():
     lib.orc_volume.argtypes = [C.c_void_p]
     lib.orc_logdet_even.restype = C.c_double
     lib.orc_logdet_even.argtypes = [C.c_void_p]
+    lib.orc_logdet_odd.restype = C.c_double
+    lib.orc_logdet_odd.argtypes = [C.c_void_p]
     lib.orc_neg_eigs.argtypes = [C.c_void_p]
     lib.orc_get_clover.argtypes = [C.c_void_p, dp, dp]
     lib.orc_clover_invert_packed.restype = C.c_double
@@ -245,6 +247,9 @@ class OracleOp:
 
     def logdet_even(self):
         return self.lib.orc_logdet_even(self.h)
+
+    def logdet_odd(self):
+        return self.lib.orc_logdet_odd(self.h)
 
     def neg_eigs(self):
         return self.lib.orc_neg_eigs(self.h)

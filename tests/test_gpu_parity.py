@@ -47,6 +47,10 @@ def test_clover_build_matches(setup):
     assert rel(ci[par == 0], oci[par == 0]) < 1e-12
     assert abs(ld - op.logdet_even()) < 1e-10 * abs(op.logdet_even())
     assert nn == op.neg_eigs()
+    # the symmetric operator's odd-site log det (logDetOddOddLinOp) beside the even one
+    le, lo = ctx.logdet()
+    assert le == ld
+    assert abs(lo - op.logdet_odd()) < 1e-10 * abs(op.logdet_odd())
 
 
 @pytest.mark.parametrize("prec", [G.PREC_DOUBLE, G.PREC_SINGLE, G.PREC_HALF], ids=["f64", "f32", "f16"])
