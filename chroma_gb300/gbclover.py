@@ -22,6 +22,9 @@ RECON_18, RECON_12 = 18, 12
 OP_DSLASH, OP_CLOVER, OP_CLOVINV, OP_MEO, OP_MDAGM, OP_UNPREC, OP_SYM, OP_SYM_MDAGM = range(8)
 SOLVER_CG, SOLVER_RELIABLE_CG, SOLVER_MIXED, SOLVER_FGMRES, SOLVER_BICGSTAB = range(5)
 SYS_MEO, SYS_MDAGM, SYS_FULL, SYS_SYM, SYS_SYM_MDAGM = range(5)
+# status codes (GBC_OK, GBC_ERR_*)
+(OK, ERR_ARGS, ERR_CUDA, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_NONFINITE, ERR_STATE, ERR_RECON,
+ ERR_PRECOND) = range(9)
 
 # every entry point include/gbclover.h declares
 EXPORTS = ["gbc_create", "gbc_destroy", "gbc_strerror", "gbc_last_error", "gbc_load_gauge", "gbc_load_clover",

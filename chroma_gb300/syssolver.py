@@ -15,7 +15,8 @@ Mirrors, for Python callers and for the tests, the interface that the C++ adapte
 - ``PrecFermActQprop``: the full-lattice propagator solve (eoprec_fermact_qprop.cc:41-80).
 Failure handling follows syssolver_linop_clover_quda_w.h:636-643: a relative residual above
 RsdToleranceFactor * RsdTarget raises ``SolverFailure`` unless SilentFail is set, and a
-BackupSolverParam group runs the backup solver instead.
+BackupSolverParam group runs the backup solver instead (Chroma's QUDA clover solver reads that
+group, syssolver_quda_clover_params.cc:105-115, but never runs it).
 """
 import xml.etree.ElementTree as ET
 from dataclasses import dataclass, field
@@ -144,6 +145,7 @@ class SysSolverGB300CloverParams:
 class _Base:
     system = G.SYS_MEO
     symmetric_system = None
+    runs_backup = True  # the LinOp solvers run BackupSolverParam; the MdagM solver does not
 
     def __init__(self, links, dims, params: SysSolverGB300CloverParams, max_rhs=12, operator="EOPREC_CLOVER"):
         """operator: the FermAct whose LinearOperator the solver inverts; "SEOPREC_CLOVER" selects the
@@ -183,14 +185,19 @@ class _Base:
                    for r in res]
         bad = [r for r in results if r.status != 0]
         if bad:
-            if p.BackupSolverParam:
+            if p.BackupSolverParam and self.runs_backup:
+                # the backup solves the same system on this context; its iterations add to the
+                # failed solve's, as in the C++ adapter
                 backup = SysSolverGB300CloverParams.from_xml(p.BackupSolverParam)
                 backup.CloverParams = p.CloverParams
                 saved, self.params = self.params, backup
                 try:
-                    return self._solve(psi, chi)
+                    psi_out, res2 = self._solve(psi, chi)
                 finally:
                     self.params = saved
+                for a, b in zip(res2 if multi else [res2], results):
+                    a.n_count += b.n_count
+                return psi_out, res2
             if not p.SilentFail:
                 raise SolverFailure(f"GB300_CLOVER_INVERTER failed: {bad[0]}")
         psi_out = out.reshape(np.asarray(chi).shape)
@@ -212,6 +219,7 @@ class MdagMSysSolverGB300Clover(_Base):
     M_s^dag M_s psi = chi for a SEOPREC_CLOVER action."""
     system = G.SYS_MDAGM
     symmetric_system = G.SYS_SYM_MDAGM
+    runs_backup = False
 
     def __call__(self, psi, chi, predictor=None):
         if predictor is not None:
