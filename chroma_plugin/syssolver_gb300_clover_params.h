@@ -29,7 +29,7 @@ namespace Chroma
     CloverFermActParams CloverParams;
     bool AntiPeriodicT;
     Real Delta;
-    std::string SolverType;           // CG | RELIABLE_CG | MIXED | FGMRES (BICGSTAB, GCR -> MIXED)
+    std::string SolverType;           // CG | RELIABLE_CG | MIXED | BICGSTAB | FGMRES (GCR -> FGMRES)
     std::string CudaSloppyPrecision;  // HALF | SINGLE | DOUBLE
     std::string CudaSloppyReconstruct;// RECONS_12 | RECONS_NONE
     Real RsdToleranceFactor;
