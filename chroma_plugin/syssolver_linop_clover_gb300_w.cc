@@ -3,6 +3,8 @@
  */
 #include "chroma_plugin/syssolver_linop_clover_gb300_w.h"
 
+#include <sstream>
+
 #include "actions/ferm/invert/syssolver_linop_factory.h"
 #include "actions/ferm/invert/syssolver_mdagm_factory.h"
 #include "actions/ferm/linop/seoprec_clover_linop_w.h"
