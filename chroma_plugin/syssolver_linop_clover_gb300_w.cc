@@ -8,6 +8,7 @@
 #include "actions/ferm/invert/syssolver_linop_factory.h"
 #include "actions/ferm/invert/syssolver_mdagm_factory.h"
 #include "actions/ferm/linop/seoprec_clover_linop_w.h"
+#include "lmdagm.h"
 
 namespace Chroma
 {

@@ -1,3 +1,10 @@
-// compile-only stand-in (see chroma_stand_in.h)
+// compile-only stand-in: the declarations the adapter takes from this header
 #pragma once
-#include "../../../chroma_stand_in.h"
+#include "../../../linearop.h"
+#include "../../../handle.h"
+#include "../../../syssolver.h"
+
+namespace Chroma {
+template <typename T>
+class LinOpSystemSolver : public SystemSolver<T> {};
+}  // namespace Chroma

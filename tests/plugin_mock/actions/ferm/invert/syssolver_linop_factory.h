@@ -1,3 +1,10 @@
-// compile-only stand-in (see chroma_stand_in.h)
+// compile-only stand-in: the declarations the adapter takes from this header
 #pragma once
-#include "../../../chroma_stand_in.h"
+#include "syssolver_linop.h"
+#include "../../../state.h"
+#include "../../../handle.h"
+#include "../../../factory_stand_in.h"
+
+namespace Chroma {
+typedef Singleton<SolverFactory<LinOpSystemSolver<LatticeFermion> > > TheLinOpFermSystemSolverFactory;
+}  // namespace Chroma

@@ -1,3 +1,11 @@
-// compile-only stand-in (see chroma_stand_in.h)
+// compile-only stand-in: the declarations the adapter takes from this header
 #pragma once
-#include "../../../chroma_stand_in.h"
+#include "../../../linearop.h"
+
+namespace Chroma {
+class SymEvenOddPrecCloverLinOp : public LinearOperator<LatticeFermion> {
+ public:
+  void operator()(LatticeFermion& chi, const LatticeFermion& psi, enum PlusMinus isign) const override;
+  const Subset& subset() const override;
+};
+}  // namespace Chroma

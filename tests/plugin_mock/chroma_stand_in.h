@@ -1,4 +1,6 @@
-// Compile-only stand-ins for the parts of QDP++ and Chroma that chroma_plugin/ uses.
+// Compile-only stand-ins for the parts of QDP++ (and chromabase.h) that chroma_plugin/ uses; the
+// Chroma declarations sit in stand-ins named like the Chroma headers that declare them, so that a
+// missing #include in the adapter fails here as it would in a Chroma build.
 //
 // Test infrastructure: tests/test_plugin_compiles.py compiles the adapter sources against these
 // declarations with g++ -fsyntax-only, so that the adapter's use of include/gbclover.h (types,
@@ -41,6 +43,7 @@ struct Layout {
 };
 
 struct Subset {};
+enum PlusMinus { PLUS = 1, MINUS = -1 };
 
 // element access of a lattice field: f.elem(site) ... .real() / .imag()
 struct RComplexRef {
@@ -102,116 +105,4 @@ struct QDPIO {
 
 namespace Chroma {
 using namespace QDP;
-
-template <typename T>
-class Handle {
- public:
-  Handle() = default;
-  explicit Handle(T* p) : p_(p) {}
-  T* operator->() const { return p_; }
-  T& operator*() const { return *p_; }
- private:
-  T* p_ = nullptr;
-};
-
-enum PlusMinus { PLUS = 1, MINUS = -1 };
-
-template <typename T>
-class LinearOperator {
- public:
-  virtual ~LinearOperator() {}
-  virtual void operator()(T& chi, const T& psi, enum PlusMinus isign) const = 0;
-  virtual const Subset& subset() const = 0;
-};
-
-template <typename T>
-class MdagMLinOp : public LinearOperator<T> {
- public:
-  explicit MdagMLinOp(const Handle<LinearOperator<T> >& A);
-  void operator()(T& chi, const T& psi, enum PlusMinus isign) const override;
-  const Subset& subset() const override;
-};
-
-template <typename T, typename P, typename Q>
-class FermState {
- public:
-  virtual ~FermState() {}
-  virtual const Q& getLinks() const = 0;
-};
-
-struct SystemSolverResults_t {
-  int n_count = 0;
-  Real resid;
-};
-
-template <typename T>
-class SystemSolver {
- public:
-  virtual ~SystemSolver() {}
-  virtual SystemSolverResults_t operator()(T& psi, const T& chi) const = 0;
-  virtual const Subset& subset() const = 0;
-};
-
-template <typename T>
-class LinOpSystemSolver : public SystemSolver<T> {};
-
-template <typename T>
-class AbsChronologicalPredictor4D {
- public:
-  virtual ~AbsChronologicalPredictor4D() {}
-  virtual void operator()(T& psi, const LinearOperator<T>& A, const T& chi) = 0;
-  virtual void reset() = 0;
-  virtual void newVector(const T& psi) = 0;
-};
-
-template <typename T>
-class MdagMSystemSolver : public SystemSolver<T> {
- public:
-  virtual SystemSolverResults_t operator()(T& psi, const T& chi) const = 0;
-  virtual SystemSolverResults_t operator()(T& psi, const T& chi, AbsChronologicalPredictor4D<T>& predictor) const = 0;
-};
-
-struct GroupXML_t {
-  std::string xml, id, path;
-};
-GroupXML_t readXMLGroup(XMLReader& xml, const std::string& path, const std::string& type_name);
-
-struct AnisoParam_t {
-  bool anisoP = false;
-  int t_dir = 3;
-  Real xi_0, nu;
-};
-
-struct CloverFermActParams {
-  Real Mass, clovCoeffR, clovCoeffT, u0;
-  AnisoParam_t anisoParam;
-  Real max_norm;
-  bool max_norm_usedP = false;
-  Real twisted_m;
-  bool twisted_m_usedP = false;
-};
-void read(XMLReader&, const std::string&, CloverFermActParams&);
-void write(XMLWriter&, const std::string&, const CloverFermActParams&);
-
-// string-keyed factory singletons (objfactory.h, singleton.h)
-typedef Handle<FermState<LatticeFermion, multi1d<LatticeColorMatrix>, multi1d<LatticeColorMatrix> > > FSHandle;
-template <typename Product>
-struct SolverFactory {
-  typedef Product* (*Creator)(XMLReader&, const std::string&, FSHandle, Handle<LinearOperator<LatticeFermion> >);
-  bool registerObject(const std::string& id, Creator c);
-  Product* createObject(const std::string& id, XMLReader& xml, const std::string& path, FSHandle state,
-                        Handle<LinearOperator<LatticeFermion> > A);
-};
-template <typename F>
-struct Singleton {
-  static F& Instance();
-};
-typedef Singleton<SolverFactory<LinOpSystemSolver<LatticeFermion> > > TheLinOpFermSystemSolverFactory;
-typedef Singleton<SolverFactory<MdagMSystemSolver<LatticeFermion> > > TheMdagMFermSystemSolverFactory;
-
-class SymEvenOddPrecCloverLinOp : public LinearOperator<LatticeFermion> {
- public:
-  void operator()(LatticeFermion& chi, const LatticeFermion& psi, enum PlusMinus isign) const override;
-  const Subset& subset() const override;
-};
 }  // namespace Chroma

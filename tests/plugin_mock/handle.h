@@ -1,3 +1,16 @@
-// compile-only stand-in (see chroma_stand_in.h)
+// compile-only stand-in: the declarations the adapter takes from this header
 #pragma once
-#include "chroma_stand_in.h"
+#include "chromabase.h"
+
+namespace Chroma {
+template <typename T>
+class Handle {
+ public:
+  Handle() = default;
+  explicit Handle(T* p) : p_(p) {}
+  T* operator->() const { return p_; }
+  T& operator*() const { return *p_; }
+ private:
+  T* p_ = nullptr;
+};
+}  // namespace Chroma

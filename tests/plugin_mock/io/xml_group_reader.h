@@ -1,3 +1,10 @@
-// compile-only stand-in (see chroma_stand_in.h)
+// compile-only stand-in: the declarations the adapter takes from this header
 #pragma once
-#include "../chroma_stand_in.h"
+#include "../chromabase.h"
+
+namespace Chroma {
+struct GroupXML_t {
+  std::string xml, id, path;
+};
+GroupXML_t readXMLGroup(XMLReader& xml, const std::string& path, const std::string& type_name);
+}  // namespace Chroma
