@@ -28,3 +28,19 @@ def test_check_catches_an_abi_mismatch(tmp_path):
     bad.write_text('#include "gbclover.h"\nint f(gbc_ctx* c, double* p) { return gbc_solve(c, nullptr, 1, p, p); }\n')
     r = subprocess.run([CXX, *FLAGS, str(bad)], capture_output=True, text=True)
     assert r.returncode != 0 and "gbc_solve" in r.stderr
+
+
+def test_abi_header_is_plain_c99(tmp_path):
+    # callers in C (or any FFI that parses C) include the header without a C++ compiler
+    cc = os.environ.get("CC") or shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "caller.c"
+    src.write_text('#include "gbclover.h"\n'
+                   'int main(void) {\n'
+                   '  gbc_ctx* c = 0; gbc_solve_params p = {0}; gbc_result r; double x = 0;\n'
+                   '  return gbc_solve(c, &p, 1, &x, &x, &r) + gbc_get_logdet(c, &x, 0);\n'
+                   '}\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only",
+                        "-I", os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
