@@ -9,6 +9,9 @@ GPU library are checked against the same fixed numbers:
   gives the same field);
 - ``src``: a Gaussian source on the odd sites (numpy PCG64, seed 7);
 - ``meo``, ``meo_dag``: M~ src and M~^dag src (eoprec_clover_linop_w.cc:142-187);
+- ``msym``: M_s src, the symmetric operator 1 - 1/4 A_oo^-1 D_oe A_ee^-1 D_eo
+  (seoprec_clover_linop_w.cc:145-187);
+- ``meo_tw``: M~ src with a twisted-mass term TwistedM = 0.05 (eoprec_clover_linop_w.cc:174-184);
 - ``psi``: the solution of M~ psi = src by CGNE to a relative residual of 1e-13 (invcg2.cc:70-232);
 - ``logdet_even``, ``logdet_odd``: sum of log|d| of the clover blocks' LDL^dag factors.
 Spinors hold the odd sites only, in increasing site index ``x + Lx*(y + Ly*(z + Lz*t))``.
@@ -25,6 +28,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 DIMS = (4, 4, 4, 4)
 KAPPA, CSW, EPS, SEED, SRC_SEED = 0.115, 1.2, 0.3, 2024, 7
+TWISTED_M = 0.05
 PATH = os.path.join(HERE, "eoclover_4x4x4x4.npz")
 
 
@@ -65,10 +69,13 @@ def main():
     src = source()
     meo = op.apply(O.OP_MEO, full(src), +1, 1)[odd]
     meo_dag = op.apply(O.OP_MEO, full(src), -1, 1)[odd]
+    msym = op.apply(O.OP_SYM, full(src), +1, 1)[odd]
+    tw = OracleOp(DIMS, u, 1 / (2 * KAPPA) - 4, CSW, twisted_m=TWISTED_M)
+    meo_tw = tw.apply(O.OP_MEO, full(src), +1, 1)[odd]
     psi, res = op.solve(full(src), solver=O.SOLVER_CG, rsd=1e-13, maxit=10000)
     np.savez_compressed(PATH, dims=np.array(DIMS, dtype=np.int32), kappa=KAPPA, csw=CSW, eps=EPS, seed=SEED,
                         src_seed=SRC_SEED, plaquette=np.array(orc.plaquette(DIMS, u), dtype=np.float64),
-                        src=src, meo=meo, meo_dag=meo_dag, psi=psi[odd], rel_resid=res["rel_resid"],
+                        src=src, meo=meo, meo_dag=meo_dag, msym=msym, meo_tw=meo_tw, psi=psi[odd], rel_resid=res["rel_resid"],
                         logdet_even=op.logdet_even(), logdet_odd=op.logdet_odd())
     print(PATH, res)
 

@@ -1,6 +1,7 @@
 """Golden vectors of the even-odd clover operator and its solve (tests/golden/eoclover_4x4x4x4.npz,
 made by tests/golden/make_oracle_fixture.py): the oracle rebuilt on this host, and the GPU library
-through the C ABI, reproduce the recorded M~ src, M~^dag src, solution and clover log dets.
+through the C ABI, reproduce the recorded M~ src, M~^dag src, solution and clover log dets; the
+oracle also the symmetric and the twisted-mass operator.
 
 Tolerances: the seeded links to 1e-14 (plaquette); FP64 operators 1e-12 relative; log dets 1e-12
 relative; the oracle's solution to 1e-12 residual within 1e-9 of the golden one, the GPU's (plain
@@ -47,6 +48,9 @@ def test_oracle_reproduces_golden():
     src = F.full(GOLD["src"])
     assert rel(op.apply(O.OP_MEO, src, +1, 1)[odd], GOLD["meo"]) < 1e-12
     assert rel(op.apply(O.OP_MEO, src, -1, 1)[odd], GOLD["meo_dag"]) < 1e-12
+    assert rel(op.apply(O.OP_SYM, src, +1, 1)[odd], GOLD["msym"]) < 1e-12
+    tw = OracleOp(F.DIMS, _links(), 1 / (2 * F.KAPPA) - 4, F.CSW, twisted_m=F.TWISTED_M)
+    assert rel(tw.apply(O.OP_MEO, src, +1, 1)[odd], GOLD["meo_tw"]) < 1e-12
     psi, res = op.solve(src, solver=O.SOLVER_CG, rsd=1e-12, maxit=10000)
     assert rel(psi[odd], GOLD["psi"]) < 1e-9
     assert abs(op.logdet_even() - GOLD["logdet_even"]) < 1e-12 * abs(GOLD["logdet_even"])
