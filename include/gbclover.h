@@ -142,6 +142,9 @@ typedef struct gbc_ctx gbc_ctx;
 int gbc_create(gbc_ctx** ctx, const gbc_geom* geom, const gbc_action* act, const gbc_opts* opts);
 /* Replaces ~LinOpSysSolverQUDAClover (syssolver_linop_clover_quda_w.h:570-575). */
 void gbc_destroy(gbc_ctx* ctx);
+/* Text of a status code, and the message of the context's last failure.  Chroma reports a failed
+   solve on QDPIO::cerr before QDP_abort (syssolver_linop_clover_quda_w.h:636-643); the adapter
+   prints these strings there. */
 const char* gbc_strerror(int status);
 const char* gbc_last_error(gbc_ctx* ctx);
 /* The stencil launch shapes the autotuner picked so far, one line per kernel configuration
