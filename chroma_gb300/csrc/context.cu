@@ -447,9 +447,11 @@ const char* gbc_tune_report(gbc_ctx* c) { return c ? c->tune_log.c_str() : ""; }
 int gbc_create(gbc_ctx** out, const gbc_geom* geom, const gbc_action* act, const gbc_opts* opts) {
   if (!out || !geom || !act) return GBC_ERR_ARGS;
   *out = nullptr;
+  // every extent even (QDP++'s rb checkerboard needs it): with an odd extent the wrap-around
+  // neighbour in that direction has the site's own parity and the checkerboarded stencil would
+  // read the wrong field
   for (int m = 0; m < 4; ++m)
-    if (geom->dims[m] < 2) return GBC_ERR_ARGS;
-  if (geom->dims[0] % 2) return GBC_ERR_ARGS;
+    if (geom->dims[m] < 2 || geom->dims[m] % 2) return GBC_ERR_ARGS;
   if (geom->t_boundary != 1 && geom->t_boundary != -1) return GBC_ERR_ARGS;
   long V = (long)geom->dims[0] * geom->dims[1] * geom->dims[2] * geom->dims[3];
   if (V / 2 > (1L << 30)) return GBC_ERR_ARGS;
@@ -481,6 +483,9 @@ int gbc_create(gbc_ctx** out, const gbc_geom* geom, const gbc_action* act, const
         if (m != act->t_dir) c->link_coeff[m] = act->nu / act->xi_0;
     }
     GBC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    // the static scratch of gbc_apply_meo_noalloc is reserved on this device now, while the caller
+    // sets up, rather than on that entry point's first call (the library's modules load lazily)
+    if (noalloc_reserve() != GBC_OK) throw CudaError{cudaErrorMemoryAllocation, "noalloc scratch reservation"};
     // reduction partials: the largest grid is the hopping kernel with 16 sites per block
     c->part_stride = (g.Vh + 15) / 16;
     if (c->part_stride < blas_blocks(g)) c->part_stride = blas_blocks(g);

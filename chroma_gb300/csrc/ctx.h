@@ -141,6 +141,10 @@ struct SymScope {
 void sync(gbc_ctx* c);
 double now();
 
+// ---- no-allocation operator (noalloc.cu) ---------------------------------------------------------
+// makes gbc_apply_meo_noalloc's static scratch exist on the current device (loads its module)
+int noalloc_reserve();
+
 // ---- learned preconditioner (precond.cu) ----------------------------------------------------
 void precond_free(gbc_ctx* c);
 // out ~= M~^-1 in (odd checkerboard fields, same precision, nrhs right-hand sides)

@@ -172,8 +172,13 @@ __global__ void noalloc_odd(CanonGeom g, const double2* links, const double* clo
   }
 }
 
-// Device address of the scratch array on the current device; looked up once per device.
-int scratch_for_current_device(double2** out) {
+}  // namespace
+
+// Device address of the scratch array on the current device; looked up once per device.  The
+// lookup is also what makes the array exist there: under CUDA's default lazy module loading
+// (CUDA_MODULE_LOADING=LAZY) this file's module, with its static array, is loaded on the first
+// use of one of its symbols, not when the library is loaded.
+int noalloc_scratch_for_current_device(double2** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GBC_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_mu);
@@ -191,7 +196,11 @@ int scratch_for_current_device(double2** out) {
   return GBC_OK;
 }
 
-}  // namespace
+int noalloc_reserve() {
+  double2* p = nullptr;
+  return noalloc_scratch_for_current_device(&p);
+}
+
 }  // namespace gbc
 
 extern "C" int gbc_apply_meo_noalloc(const gbc_geom* geom, const gbc_action* act, const double* links_dev,
@@ -200,9 +209,9 @@ extern "C" int gbc_apply_meo_noalloc(const gbc_geom* geom, const gbc_action* act
   using namespace gbc;
   if (!geom || !act || !links_dev || !clov_dev || !invclov_dev || !out_dev || !in_dev) return GBC_ERR_ARGS;
   if (isign != 1 && isign != -1) return GBC_ERR_ARGS;
+  // every extent even: with an odd extent the wrap-around neighbour has the site's own parity
   for (int m = 0; m < 4; ++m)
-    if (geom->dims[m] < 2) return GBC_ERR_ARGS;
-  if (geom->dims[0] % 2) return GBC_ERR_ARGS;
+    if (geom->dims[m] < 2 || geom->dims[m] % 2) return GBC_ERR_ARGS;
   const long V = (long)geom->dims[0] * geom->dims[1] * geom->dims[2] * geom->dims[3];
   if (V / 2 > GBC_NOALLOC_MAX_VH) {
     fprintf(stderr,
@@ -212,7 +221,7 @@ extern "C" int gbc_apply_meo_noalloc(const gbc_geom* geom, const gbc_action* act
     return GBC_ERR_ARGS;
   }
   double2* scratch = nullptr;
-  int rc = scratch_for_current_device(&scratch);
+  int rc = noalloc_scratch_for_current_device(&scratch);
   if (rc != GBC_OK) return rc;
   CanonGeom g;
   for (int m = 0; m < 4; ++m) g.L[m] = geom->dims[m];

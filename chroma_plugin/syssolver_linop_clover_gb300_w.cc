@@ -3,6 +3,7 @@
  */
 #include "chroma_plugin/syssolver_linop_clover_gb300_w.h"
 
+#include <limits>
 #include <sstream>
 
 #include "actions/ferm/invert/syssolver_linop_factory.h"
@@ -162,13 +163,19 @@ namespace Chroma
       dev.gather(hchi, chi);
       dev.gather(hpsi, psi);
       gbc_solve_params q = make_params(p, system);
-      gbc_result r;
+      // a call refused before the solve starts (bad arguments, call order, CUDA error) fills no
+      // result and leaves psi as it was: report no iterations and an unknown residual then
+      gbc_result r{};
+      r.resid = r.rel_resid = std::numeric_limits<double>::quiet_NaN();
       int rc = gbc_solve(dev.get(), &q, 1, hpsi.data(), hchi.data(), &r);
       dev.scatter(psi, hpsi, 2);  // rb[1] only
       SystemSolverResults_t res;
       res.n_count = r.n_count;
       res.resid = r.resid;
       failed = rc != GBC_OK;
+      if (failed)
+        QDPIO::cerr << "GB300_CLOVER_INVERTER: " << gbc_strerror(rc) << ": " << gbc_last_error(dev.get())
+                    << std::endl;
       QDPIO::cout << "GB300_CLOVER_INVERTER: " << r.n_count << " iterations (" << r.n_outer << " outer). Rsd = "
                   << r.resid << " Relative Rsd = " << r.rel_resid << " time " << r.seconds << " s" << std::endl;
       return res;

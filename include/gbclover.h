@@ -80,7 +80,7 @@ extern "C" {
 
 /* ---- parameter structs ------------------------------------------------------------------- */
 typedef struct gbc_geom {
-  int dims[4];    /* Lx, Ly, Lz, Lt; Lx even, every extent >= 2 */
+  int dims[4];    /* Lx, Ly, Lz, Lt; every extent even and >= 2 (QDP++'s rb checkerboard) */
   int t_boundary; /* +1 periodic, -1 antiperiodic in time: the sign already folded into the links
                      at t = Lt-1 (SimpleFermBC::modify, simple_fermbc.h:87-104); used by the
                      12-real reconstruction */
@@ -218,10 +218,13 @@ int gbc_time_operator(gbc_ctx* ctx, int op, int prec, int nrhs, int iters, int f
    on the odd sites; invclov_dev: packed A^-1 on the even sites; in_dev/out_dev: full-lattice
    spinors, odd sites read/written, even sites of out_dev untouched).  Its one temporary, the
    even-parity intermediate, lives in a static device array of GBC_NOALLOC_MAX_VH sites per
-   checkerboard (12 MiB) that every GPU which loads the library holds until exit.  Lattices with
-   more than GBC_NOALLOC_MAX_VH sites per checkerboard return GBC_ERR_ARGS with a message on
-   stderr.  The first call on a device looks up that array's device address (once per device,
-   with the device current), so make the first call before any stream capture.  Work is issued
+   checkerboard (12 MiB).  CUDA loads the library's modules lazily by default, so that array is
+   taken on a device when the first gbc_create or gbc_apply_meo_noalloc runs there (with that
+   device current), and held until exit: a caller whose allocator will later hold the GPU makes
+   one of those calls first.  Lattices with more than GBC_NOALLOC_MAX_VH sites per checkerboard,
+   or an odd extent, return GBC_ERR_ARGS (the size case with a message on stderr).  The first
+   call on a device also looks up that array's device address (once per device), so make the
+   first call before any stream capture.  Work is issued
    on `stream` (a cudaStream_t; NULL = the default stream); every call shares the one array, so
    calls that overlap on the GPU race -- serialise them. */
 #define GBC_NOALLOC_MAX_VH 65536

@@ -6,7 +6,7 @@ The npz keeps the parsed header fields and the raw big-endian payload bytes, so 
 tests can rebuild an archive byte stream and exercise the oracle's reader and the
 12-real reconstruction without the Chroma tree being present.
 
-Usage:  python tests/golden/make_nersc_fixture.py [path/to/chroma]
+Usage:  python tests/golden/make_nersc_fixture.py path/to/chroma   (the root of a Chroma source tree)
 """
 import os
 import sys
@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main(chroma_root="/root/reference"):
+def main(chroma_root):
     path = os.path.join(chroma_root, "tests", "t_asqtad_prop", "t_nersc.cfg")
     raw = open(path, "rb").read()
     end = raw.index(b"END_HEADER")
@@ -38,4 +38,6 @@ def main(chroma_root="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    main(sys.argv[1])

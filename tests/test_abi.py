@@ -42,12 +42,21 @@ def test_strerror(lib):
     assert lib.gbc_strerror(3) == b"solver did not converge"
 
 
-def test_create_rejects_bad_geometry(lib):
+@pytest.mark.parametrize("dims", [(3, 4, 4, 4), (4, 3, 4, 4), (4, 4, 5, 4), (4, 4, 4, 7), (4, 4, 4, 1)])
+def test_create_rejects_odd_or_short_extent(lib, dims):
+    # QDP++'s rb checkerboard needs every extent even: with an odd extent the wrap-around
+    # neighbour has the site's own parity; the check runs before any CUDA call
     h = C.c_void_p()
-    g = G.Geom((C.c_int * 4)(3, 4, 4, 4), -1)  # odd Lx
+    g = G.Geom((C.c_int * 4)(*dims), -1)
     a = G.Action(0.1, 1.0, 1.0, 0, 1.0, 1.0, 3, 0, 0.0)
     assert lib.gbc_create(C.byref(h), C.byref(g), C.byref(a), None) == 1
-    g = G.Geom((C.c_int * 4)(4, 4, 4, 4), 0)  # bad boundary
+    assert not h.value
+
+
+def test_create_rejects_bad_boundary(lib):
+    h = C.c_void_p()
+    a = G.Action(0.1, 1.0, 1.0, 0, 1.0, 1.0, 3, 0, 0.0)
+    g = G.Geom((C.c_int * 4)(4, 4, 4, 4), 0)
     assert lib.gbc_create(C.byref(h), C.byref(g), C.byref(a), None) == 1
 
 

@@ -6,7 +6,7 @@ library's only temporary is a static device array.
 Checked through the C ABI against gbc_apply(GBC_OP_MEO, FP64) -- the ordinary entry point, whose
 workspaces live in a context -- at the FP64 tolerance of the operator tests (1e-12 relative), on
 two calls in a row with different inputs (the static scratch keeps the previous call's data, which
-must not leak into the next result), for both signs.  Kept in a file of its own that pytest
+must not leak into the next result), for both signs, with and without a twisted-mass term.  Kept in a file of its own that pytest
 collects last."""
 import ctypes as C
 
@@ -23,14 +23,16 @@ def _rel(a, b):
     return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
 
 
-def test_noalloc_meo_matches_gbc_apply():
+@pytest.mark.parametrize("twisted_m", [None, 0.05])
+def test_noalloc_meo_matches_gbc_apply(twisted_m):
+    """Plain clover and a twisted-mass term (+ isign i mu gamma_5, whose sign flips with isign)."""
     import torch
     dims = (8, 8, 8, 8)
     kappa, csw = 0.115, 1.0
     mass = 1 / (2 * kappa) - 4
     V = int(np.prod(dims))
     links = G.gauge_synthetic(dims, 0.3, 4242, t_boundary=-1)
-    ctx = G.Context(dims, mass, csw, t_boundary=-1, max_rhs=2)
+    ctx = G.Context(dims, mass, csw, t_boundary=-1, max_rhs=2, twisted_m=twisted_m)
     try:
         ctx.load_gauge(links)
         clov, inv, _, _ = ctx.get_clover()
@@ -38,7 +40,7 @@ def test_noalloc_meo_matches_gbc_apply():
         lib.gbc_apply_meo_noalloc.argtypes = [C.POINTER(G.Geom), C.POINTER(G.Action), C.c_void_p, C.c_void_p,
                                               C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         geom = G.Geom((C.c_int * 4)(*dims), -1)
-        act = G.Action(mass, csw, csw, 0, 1.0, 1.0, 3, 0, 0.0)
+        act = G.Action(mass, csw, csw, 0, 1.0, 1.0, 3, int(twisted_m is not None), float(twisted_m or 0.0))
         # caller-owned device buffers
         d_links = torch.from_numpy(links.view(np.float64).reshape(-1).copy()).cuda()
         d_clov = torch.from_numpy(clov.reshape(-1).copy()).cuda()
@@ -75,4 +77,19 @@ def test_noalloc_rejects_lattice_beyond_scratch():
     p = [b.data_ptr() for b in bufs]
     rc = lib.gbc_apply_meo_noalloc(C.byref(geom), C.byref(act), p[0], p[1], p[2], 1, p[3], p[4], None)
     assert rc == 1  # GBC_ERR_ARGS
+    assert torch.count_nonzero(bufs[3]).item() == 0
+
+
+@pytest.mark.parametrize("dims", [(8, 7, 8, 8), (8, 8, 8, 5)])
+def test_noalloc_rejects_odd_extent(dims):
+    lib = G.load()
+    lib.gbc_apply_meo_noalloc.argtypes = [C.POINTER(G.Geom), C.POINTER(G.Action), C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    geom = G.Geom((C.c_int * 4)(*dims), -1)
+    act = G.Action(0.0, 1.0, 1.0, 0, 1.0, 1.0, 3, 0, 0.0)
+    import torch
+    bufs = [torch.zeros(8, dtype=torch.float64, device="cuda") for _ in range(5)]
+    p = [b.data_ptr() for b in bufs]
+    rc = lib.gbc_apply_meo_noalloc(C.byref(geom), C.byref(act), p[0], p[1], p[2], 1, p[3], p[4], None)
+    assert rc == 1  # GBC_ERR_ARGS, before any kernel
     assert torch.count_nonzero(bufs[3]).item() == 0
