@@ -341,6 +341,33 @@ void iteration(gbc_ctx* c, int po, BiScal* sc, int n, const Spinor& x, const Spi
 
 }  // namespace
 
+void bicgstab_xr_update(gbc_ctx* c, int pa, int po, const double* alpha_omega, int n, const Spinor& x,
+                        const Spinor& r, const Spinor& p, const Spinor& v, const Spinor& t, const Spinor& r0) {
+  if (!((pa == PREC_DOUBLE && po == PREC_DOUBLE) || (pa == PREC_SINGLE && (po == PREC_SINGLE || po == PREC_HALF))))
+    throw std::string("BiCGStab update not built for this precision pair");
+  if (c->bisc_cap < n) {
+    if (c->d_bisc) cudaFree(c->d_bisc);
+    c->d_bisc = nullptr;
+    c->bisc_cap = 0;
+    GBC_CUDA(cudaMalloc(&c->d_bisc, sizeof(BiScal) * n));
+    c->bisc_cap = n;
+  }
+  BiScal* d_sc = static_cast<BiScal*>(c->d_bisc);
+  std::vector<BiScal> hs(n);
+  for (int i = 0; i < n; ++i) {
+    std::memset(&hs[i], 0, sizeof(BiScal));
+    hs[i].alpha = make_double2(alpha_omega[4 * i], alpha_omega[4 * i + 1]);
+    hs[i].omega = make_double2(alpha_omega[4 * i + 2], alpha_omega[4 * i + 3]);
+    hs[i].active = 1;
+  }
+  GBC_CUDA(cudaMemcpyAsync(d_sc, hs.data(), sizeof(BiScal) * n, cudaMemcpyHostToDevice, c->stream));
+  if (pa == PREC_DOUBLE) run<3>(c, n, d_sc, XRUpdF<PrecD, PrecD>{d_sc, x, r, p, v, t, r0});
+  else if (po == PREC_SINGLE) run<3>(c, n, d_sc, XRUpdF<PrecS, PrecS>{d_sc, x, r, p, v, t, r0});
+  else run<3>(c, n, d_sc, XRUpdF<PrecS, PrecH>{d_sc, x, r, p, v, t, r0});
+  GBC_CUDA(cudaGetLastError());
+  sync(c);  // hs goes out of scope
+}
+
 InnerStats bicgstab(gbc_ctx* c, int pa, int po, double tol, int maxit, double delta, const Spinor& x,
                     const Spinor& b, const std::vector<int>& active) {
   const int n = x.nrhs;

@@ -161,6 +161,12 @@ struct InnerStats {
 InnerStats bicgstab(gbc_ctx* c, int pa, int po, double tol, int maxit, double delta, const Spinor& x,
                     const Spinor& b, const std::vector<int>& active);
 
+// one fused BiCGStab update x += alpha p + omega (r - alpha v), r -= alpha v + omega t with |r|^2
+// and (r0, r) in red(c).result rows 0, 1, 2 (alpha_omega: re, im of alpha, then of omega, per
+// right-hand side); the precision pairs the inner solver uses: (FP64, FP64), (FP32, FP32), (FP32, FP16)
+void bicgstab_xr_update(gbc_ctx* c, int pa, int po, const double* alpha_omega, int n, const Spinor& x,
+                        const Spinor& r, const Spinor& p, const Spinor& v, const Spinor& t, const Spinor& r0);
+
 // ---- solvers (solvers.cu) -------------------------------------------------------------------
 // after_export (optional) runs once the solution is in psi_canon on the context stream and before
 // the final residual check, which only reads it: gbc_solve starts the copy to the host there

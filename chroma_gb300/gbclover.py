@@ -22,6 +22,7 @@ RECON_18, RECON_12 = 18, 12
 OP_DSLASH, OP_CLOVER, OP_CLOVINV, OP_MEO, OP_MDAGM, OP_UNPREC, OP_SYM, OP_SYM_MDAGM = range(8)
 SOLVER_CG, SOLVER_RELIABLE_CG, SOLVER_MIXED, SOLVER_FGMRES, SOLVER_BICGSTAB = range(5)
 SYS_MEO, SYS_MDAGM, SYS_FULL, SYS_SYM, SYS_SYM_MDAGM = range(5)
+BLAS_NORM2, BLAS_CDOT, BLAS_CG_UPDATE, BLAS_XPAY, BLAS_BICG_XR = range(5)
 # status codes (GBC_OK, GBC_ERR_*)
 (OK, ERR_ARGS, ERR_CUDA, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_NONFINITE, ERR_STATE, ERR_RECON,
  ERR_PRECOND) = range(9)
@@ -33,7 +34,7 @@ EXPORTS = ["gbc_create", "gbc_destroy", "gbc_strerror", "gbc_last_error", "gbc_l
            "gbc_precond_init", "gbc_precond_save", "gbc_precond_weights", "gbc_precond_set_weights",
            "gbc_precond_apply", "gbc_precond_loss_grad", "gbc_precond_train", "gbc_batch_create",
            "gbc_batch_destroy", "gbc_batch_solve", "gbc_batch_last_error", "gbc_stout_smear",
-           "gbc_solve_multishift"]
+           "gbc_solve_multishift", "gbc_blas"]
 
 
 class Geom(C.Structure):
@@ -116,6 +117,7 @@ def load(path=LIB_PATH):
     lib.gbc_batch_last_error.restype = C.c_char_p
     lib.gbc_batch_last_error.argtypes = [C.c_void_p]
     lib.gbc_stout_smear.argtypes = [C.POINTER(Geom), C.c_int, C.c_double, C.POINTER(C.c_int), dp, dp]
+    lib.gbc_blas.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, dp, C.POINTER(dp), dp]
     lib.gbc_solve_multishift.argtypes = [C.c_void_p, C.POINTER(SolveParams), C.c_int, dp, dp, C.POINTER(dp), dp,
                                          C.POINTER(Result)]
     _lib = lib
@@ -284,6 +286,22 @@ class Context:
         self._check(self.lib.gbc_time_operator(self.h, int(op), int(prec), int(nrhs), int(iters), int(bool(flush_l2)),
                                                C.byref(sec), C.byref(byt)), "time_operator")
         return sec.value, byt.value
+
+    def blas(self, op, fields, coef=None, prec_acc=PREC_DOUBLE, prec_op=PREC_DOUBLE):
+        """One BLAS-1 kernel of the solvers on host fields (gbc_blas); fields are updated in place.
+        Returns the reductions, shape (nrhs, nq)."""
+        fs = [self._fields(f) for f in fields]
+        for f, orig in zip(fs, fields):
+            if not np.shares_memory(f, orig):
+                raise ValueError("fields must be C-contiguous complex128 arrays (updated in place)")
+        nrhs = fs[0].shape[0]
+        nq = {BLAS_NORM2: 1, BLAS_CDOT: 2, BLAS_CG_UPDATE: 1, BLAS_XPAY: 0, BLAS_BICG_XR: 3}[op]
+        res = np.zeros(max(1, nq * nrhs))
+        cf = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64)
+        fp = (C.POINTER(C.c_double) * len(fs))(*[_dp(f.view(np.float64)) for f in fs])
+        self._check(self.lib.gbc_blas(self.h, int(op), int(prec_acc), int(prec_op), nrhs,
+                                      None if cf is None else _dp(cf), fp, _dp(res)), "blas")
+        return res[:nq * nrhs].reshape(nrhs, nq)
 
     def tune_report(self):
         return self.lib.gbc_tune_report(self.h).decode()

@@ -175,6 +175,27 @@ int gbc_get_logdet(gbc_ctx* ctx, double* logdet_even, double* logdet_odd);
    the operator runs in (GBC_PREC_DOUBLE for the FP64 path). */
 int gbc_apply(gbc_ctx* ctx, int op, int isign, int cb, int prec, int nrhs, double* out, const double* in);
 
+/* ---- BLAS-1 (parity tests of the reductions and fused updates the solvers run) -------------- */
+/* The QDP++ reductions over rb[1] that Chroma's solvers call, and the fused vector updates that
+   stand in for InvCG2's and BiCGStab's separate QDP++ expressions.  fields[k] are nrhs canonical
+   full-lattice host spinors back to back; the odd sites are used and updated fields are written
+   back there.  Each field is held in the precision the solvers keep it in: the accumulator
+   precision prec_acc (x, r, r0) or the operator precision prec_op (p, q, v, t).  res holds nq values
+   per right-hand side, res[rhs * nq + q]; coef holds the per-right-hand-side coefficients. */
+#define GBC_BLAS_NORM2 0     /* fields {x}: res = norm2(x, rb[1]) (invcg2.cc:121,165,182); nq 1, prec_op */
+#define GBC_BLAS_CDOT 1      /* fields {x, y}: res = Re, Im innerProduct(x, y, rb[1]) (invbicgstab.cc:77,106);
+                                nq 2; x in prec_acc, y in prec_op                                            */
+#define GBC_BLAS_CG_UPDATE 2 /* fields {x, p, r, q}: x += a p, r -= a q, res = norm2(r) with a = coef[rhs]
+                                (invcg2.cc:176-182); nq 1                                                     */
+#define GBC_BLAS_XPAY 3      /* fields {r, p}: p = r + b p with b = coef[rhs] (invcg2.cc:220)                */
+#define GBC_BLAS_BICG_XR 4   /* fields {x, r, p, v, t, r0}: x += alpha p + omega (r - alpha v),
+                                r -= alpha v + omega t, res = norm2(r), Re, Im innerProduct(r0, r)
+                                (invbicgstab.cc:142-160, 77); coef = re, im of alpha then of omega per
+                                right-hand side; nq 3; precision pairs (DOUBLE, DOUBLE), (SINGLE, SINGLE),
+                                (SINGLE, HALF)                                                               */
+int gbc_blas(gbc_ctx* ctx, int op, int prec_acc, int prec_op, int nrhs, const double* coef, double* const* fields,
+             double* res);
+
 /* ---- solves (LinOpSystemSolver::operator()(psi, chi), lib/syssolver.h:32-50) --------------- */
 /* psi, chi: nrhs host spinors, full lattice.  GBC_SYS_MEO / MDAGM read chi and psi on the odd
    sites and write psi there; GBC_SYS_FULL reads chi everywhere and writes psi everywhere.

@@ -297,6 +297,17 @@ class OracleOp:
             raise ValueError("bad Krylov size")
         return Vs, H, R, g, dim
 
+    def full_residuals(self, psi, chi):
+        """FP64 true relative residuals |chi_k - M psi_k| / |chi_k| of the unpreconditioned operator
+        (both parities) for every right-hand side k of psi, chi (shape (n, V, 12) or (V, 12))."""
+        psi = np.asarray(psi).reshape(-1, self.V, 12)
+        chi = np.asarray(chi).reshape(-1, self.V, 12)
+        out = []
+        for p, c in zip(psi, chi):
+            r = c - self.apply(OP_UNPREC, p)
+            out.append(float(np.sqrt(np.vdot(r, r).real / np.vdot(c, c).real)))
+        return np.array(out)
+
     def qprop(self, chi, rsd=1e-10, maxit=10000):
         chi = self._vec(chi)
         psi = np.zeros_like(chi)
