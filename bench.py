@@ -38,9 +38,10 @@ KAPPA, CSW, EPS, SEED = 0.1250, 1.6, 0.3, 20251203
 RSD = 1e-10
 DELTA = 0.01  # reliable-update threshold of the inner BiCGStab (the XML's Delta)
 INNER_TOL = 1e-5  # inner relative tolerance of each outer step (the XML's InnerTol)
-# InvCG2 iterations of one source of this workload (FP64 CGNE; the GPU FP64 CG and the oracle run
-# the same recursion).  The GPU arm re-measures it every run and reports both.
-CG_ITERS_REF = 120
+# InvCG2 iterations sampled per timed step of the CPU legs (bounded samples of the full solve)
+CPU_SAMPLE_ITERS = 12
+# ncu DRAM bytes (read + write) of one 12-RHS FP16 M~ (its two stencil launches) at 24^3x48
+M12_TRAFFIC_24 = 1228.1e6
 
 
 def parse():
@@ -60,6 +61,8 @@ def parse():
     ap.add_argument("--iters", type=int, default=3)
     ap.add_argument("--profile-timed", action="store_true",
                     help="bracket the timed solves with cudaProfilerStart/Stop (ncu --profile-from-start off)")
+    ap.add_argument("--no-oracle-check", action="store_true",
+                    help="skip the oracle's FP64 check of the solutions (residuals and one oracle solve)")
     return ap.parse_args()
 
 
@@ -185,6 +188,19 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def cg_iteration_seconds(op, chi, k):
+    """Seconds per oracle InvCG2 iteration: a k-iteration and a 2-iteration solve, so that the
+    per-solve work (M~^dag chi, the initial and final residuals) cancels."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    op.solve(chi, solver=O.SOLVER_CG, rsd=1e-30, maxit=2)
+    t2 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    op.solve(chi, solver=O.SOLVER_CG, rsd=1e-30, maxit=k)
+    tk = time.perf_counter() - t0
+    return (tk - t2) / (k - 2), tk
+
+
 def cpu_baseline(dims, links, chi_one, iters_full, nsrc, budget_s=20.0):
     """Oracle FP64 InvCG2 on the host cores: a bounded number of iterations on one source,
     extrapolated to the full 12-source solve by the measured FP64 iteration count."""
@@ -193,20 +209,76 @@ def cpu_baseline(dims, links, chi_one, iters_full, nsrc, budget_s=20.0):
     t0 = time.perf_counter()
     op = OracleOp(dims, links, 1 / (2 * KAPPA) - 4, CSW)
     setup = time.perf_counter() - t0
-    # calibrate with 2 iterations, then run as many as fit in the budget
-    t0 = time.perf_counter()
-    op.solve(chi_one, solver=O.SOLVER_CG, rsd=1e-30, maxit=2)
-    per = (time.perf_counter() - t0) / 3.0  # 2 iterations + the M~^dag and residual applications
-    k = max(2, min(200, int(budget_s / max(per, 1e-6))))
-    t0 = time.perf_counter()
-    op.solve(chi_one, solver=O.SOLVER_CG, rsd=1e-30, maxit=k)
-    dt = time.perf_counter() - t0
-    per_iter = dt / (k + 1.5)
+    # calibrate, then run as many iterations as fit in the budget
+    per, _ = cg_iteration_seconds(op, chi_one, 4)
+    k = max(4, min(200, int(budget_s / max(per, 1e-6))))
+    per_iter, dt = cg_iteration_seconds(op, chi_one, k)
     threads = O.load().orc_num_threads()
     return {"value": per_iter * iters_full * nsrc, "unit": "s", "cores": threads, "kind": "port",
-            "sample": f"{k} InvCG2 iterations of 1 of {nsrc} sources ({dt:.1f} s, oracle FP64, OpenMP); "
-                      f"extrapolated x {iters_full} iterations x {nsrc} sources; operator setup {setup:.1f} s",
+            "sample": f"{k} InvCG2 iterations of 1 of {nsrc} sources ({dt:.1f} s, oracle FP64, OpenMP), per "
+                      f"iteration from the difference to a 2-iteration solve; extrapolated x {iters_full} "
+                      f"iterations x {nsrc} sources; operator setup {setup:.1f} s",
             "seconds_per_cg_iteration": per_iter}
+
+
+def oracle_check(dims, links, src, psi):
+    """The oracle's FP64 view of the benchmark's solutions (outside the timed region): the true
+    relative residual |chi - M psi| / |chi| of every source with the oracle's unpreconditioned
+    operator, and the error of source 0 against the oracle's own FP64 solve (Chroma's InvCG2 on the
+    Schur system, target 1e-12)."""
+    from oracle import OracleOp
+    t0 = time.perf_counter()
+    op = OracleOp(dims, links, 1 / (2 * KAPPA) - 4, CSW)
+    rr = op.full_residuals(psi, src)
+    ref, info = op.qprop(src[0], rsd=1e-12)
+    err = float(np.linalg.norm(psi[0] - ref) / np.linalg.norm(ref))
+    return {"oracle_true_rel_resid_max": float(rr.max()), "oracle_true_rel_resid_min": float(rr.min()),
+            "rel_error_vs_oracle_src0": err, "oracle_solve": {"iterations": info["n_count"],
+                                                              "rel_resid": info["rel_resid"]},
+            "seconds": time.perf_counter() - t0}, op
+
+
+def chroma_factory_path(ctx, G, op, src, solve_kw):
+    """What a factory-only Chroma input gets: quarkProp4_a calls the solver once per source, and
+    PrecFermActQprop (eoprec_fermact_qprop.cc:41-80) prepares each source and reconstructs the even
+    sites on the host around a LinOp solve of M~ psi_o = chi_o, which the adapter hands to gbc_solve
+    with nrhs = 1.  The host steps are timed with the oracle's OpenMP operator standing in for
+    QDP++ (the adapter's own gather/scatter loops are not included); the device solves are timed
+    through gbc_solve with host buffers."""
+    import ctypes as C
+    from oracle import oracle as O
+    nsrc = src.shape[0]
+    host = 0.0
+    dev = 0.0
+    p = G.SolveParams(solve_kw["solver"], G.SYS_MEO, RSD, 10000, DELTA, 10.0, G.PREC_HALF, INNER_TOL, 0, 16, 0, 1)
+    iters = []
+    for k in range(nsrc):
+        chi = src[k]
+        t0 = time.perf_counter()
+        t1 = op.apply(O.OP_CLOVER_INV, chi, +1, 0)
+        t2 = op.apply(O.OP_DSLASH, t1, +1, 1)
+        chi_tmp = np.ascontiguousarray(chi + 0.5 * t2)  # chi_o - D_oe A_ee^-1 chi_e, D_oe = -1/2 D'
+        host += time.perf_counter() - t0
+        psi = np.zeros_like(chi_tmp)
+        res = (G.Result * 1)()
+        t0 = time.perf_counter()
+        rc = ctx.lib.gbc_solve(ctx.h, C.byref(p), 1, psi.ctypes.data_as(C.POINTER(C.c_double)),
+                               chi_tmp.ctypes.data_as(C.POINTER(C.c_double)), res)
+        dev += time.perf_counter() - t0
+        if rc != 0:
+            raise RuntimeError(f"factory-path solve failed: {rc}")
+        iters.append(res[0].n_count)
+        t0 = time.perf_counter()
+        t1 = op.apply(O.OP_DSLASH, psi, +1, 0)
+        t2 = op.apply(O.OP_CLOVER_INV, chi + 0.5 * t1, +1, 0)  # psi_e = A_ee^-1 (chi_e - D_eo psi_o)
+        r = op.apply(O.OP_UNPREC, psi + t2) - chi  # the residual PrecFermActQprop reports
+        float(np.vdot(r, r).real)
+        host += time.perf_counter() - t0
+    return {"device_solves_s": dev, "host_schur_s": host, "total_s": dev + host,
+            "inner_iterations_per_source": iters,
+            "what": f"{nsrc} x gbc_solve(nrhs=1, GBC_SYS_MEO, host buffers) as the LinOp factory entry "
+                    "runs under quarkProp4_a; the host Schur preparation, even reconstruction and residual "
+                    "of PrecFermActQprop timed with the oracle's OpenMP operator in QDP++'s place"}
 
 
 WEIGHTS = os.path.join(ROOT, "chroma_gb300", "weights", "cnn_16x16x16x32_k0.115_csw1.0.gbcw")
@@ -287,7 +359,10 @@ def side_workloads(G):
 
 
 def run_reference(args, rank, world):
-    """--impl reference: Chroma's FP64 CG restated (the oracle) on all host cores."""
+    """--impl reference: Chroma's FP64 CG restated (the oracle) on all host cores.  One point source
+    is solved to the target first (untimed by the steps) for the iteration count and the measured
+    time of a whole single-source solve; each timed step is a bounded sample of CPU_SAMPLE_ITERS
+    InvCG2 iterations; value = seconds per iteration x iterations x 12 sources."""
     if rank != 0:
         return
     dims = tuple(int(x) for x in args.dims.split(",")) if args.dims else DIMS
@@ -297,22 +372,20 @@ def run_reference(args, rank, world):
     o = Oracle()
     links = o.apply_bc(dims, o.gauge_hot(dims, EPS, SEED), (1, 1, 1, -1))
     op = OracleOp(dims, links, 1 / (2 * KAPPA) - 4, CSW)
+    src = S.point_sources(dims).reshape(12, -1, 12)
+    t0 = time.perf_counter()
+    _, info = op.qprop(src[0], rsd=RSD)
+    one_source = time.perf_counter() - t0
+    iters_full = info["n_count"]
     # an InvCG2 iteration costs the same for any source: time it on odd-site noise
     chi = S.gaussian(dims, 1, cb=1).reshape(-1, 12)
-    iters_full = CG_ITERS_REF or 0
+    k = CPU_SAMPLE_ITERS
     per_step = []
-    k = 3
     for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        op.solve(chi, solver=O.SOLVER_CG, rsd=1e-30, maxit=k)
-        dt = time.perf_counter() - t0
+        per, _ = cg_iteration_seconds(op, chi, k)
         if i >= args.warmup:
-            per_step.append(dt / (k + 1.5))
+            per_step.append(per)
     per_iter = statistics.median(per_step)
-    if not iters_full:
-        # no recorded count: converge one source fully on the host (slow, only when not recorded)
-        _, res = op.solve(chi, solver=O.SOLVER_CG, rsd=RSD, maxit=5000)
-        iters_full = res["n_count"]
     value = per_iter * iters_full * 12
     line = {"metric": METRIC, "value": value, "unit": "s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * k * 1e3,
@@ -321,8 +394,10 @@ def run_reference(args, rank, world):
                        "solver": "Chroma's FP64 CGNE (InvCG2, CG_INVERTER) restated by the oracle, OpenMP on "
                                  "the host cores; sources one by one"},
             "cpu_baseline": {"value": value, "unit": "s", "cores": O.load().orc_num_threads(), "kind": "port",
-                             "sample": f"{k} InvCG2 iterations per step on 1 source, extrapolated x {iters_full} "
-                                       f"iterations x 12 sources"},
+                             "sample": f"{k} InvCG2 iterations per step on 1 source (per iteration from the "
+                                       f"difference to a 2-iteration solve), x {iters_full} iterations (measured: "
+                                       f"one point source solved to {RSD} in {one_source:.1f} s) x 12 sources",
+                             "one_source_solve_s": one_source, "iterations_per_source": iters_full},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -389,7 +464,7 @@ def main():
     psi_host = psi_d.cpu().numpy().view(np.complex128).reshape(nsrc, V, 12)
 
     # plain FP64 CG on the same GPU, sources one at a time (quarkProp4_a's loop)
-    plain, plain_iters, plain_res, err_vs_fp64 = None, [CG_ITERS_REF], [None], None
+    plain, plain_iters, plain_res, err_vs_fp64 = None, [], [None], None
     if args.plain_steps > 0:
         plain_t, plain_res = [], []
         for _ in range(args.plain_steps):
@@ -439,12 +514,15 @@ def main():
     secm, bytm = ctx.time_operator(G.OP_MEO, G.PREC_HALF, nrhs=1, iters=20, flush_l2=True)
     sec64, byts64 = ctx.time_operator(G.OP_DSLASH, G.PREC_DOUBLE, nrhs=1, iters=10, flush_l2=True)
     achieved = byts / sec / 1e9
-    # DRAM traffic of one such M~: ncu dram__bytes_read.sum + dram__bytes_write.sum of its two
-    # launches on 24^3x48 (1228.1 MB for Vh = 331776 sites, 12 RHS), scaled to this lattice by the
-    # number of sites (profiles/launches_propagator_32x32x32x64.md)
-    traffic = 1228.1e6 / 331776 * (V // 2)
+    # DRAM traffic of one such M~: a constant, not measured in this run (ncu cannot run inside the
+    # benchmark) -- dram__bytes_read.sum + dram__bytes_write.sum of the M~'s two launches captured
+    # once by ncu on 24^3x48 (Vh = 331776 sites, 12 RHS), scaled to this lattice by the number of
+    # sites (the traffic of a launch grows with the sites it covers)
+    traffic = M12_TRAFFIC_24 / 331776 * (V // 2)
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved / pk["hbm_gbs"], "traffic": traffic, "traffic_source": "ncu, 24^3x48 scaled by sites",
+            "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+            "traffic_source": "constant from one ncu capture of the 12-RHS M~ at 24^3x48, scaled by sites; "
+                              "not measured in this run",
             "peak_kind": pk_kind,
             "kernel": "M~ on 12 RHS, FP16 storage, 12-real links: hop_kernel_rp (A_ee^-1 D_eo) + hop_kernel_async "
                       "(A_oo x - 1/4 D_oe t), autotuned",
@@ -461,7 +539,10 @@ def main():
     e2e_t = []
     import ctypes as C
     p = G.SolveParams(G.SOLVER_BICGSTAB, G.SYS_FULL, RSD, 10000, DELTA, 10.0, G.PREC_HALF, INNER_TOL, 0, 16, 0, 1)
-    for i in range(max(1, min(args.steps, 3))):
+    # the same K steps as the device-timed loop, each through gbc_solve with pinned host buffers
+    for i in range(args.steps):
+        flush.random_()
+        torch.cuda.synchronize()
         res_arr = (G.Result * nsrc)()
         t0 = time.perf_counter()
         rc = ctx.lib.gbc_solve(ctx.h, C.byref(p), nsrc, C.cast(psi_h.data_ptr(), C.POINTER(C.c_double)),
@@ -469,14 +550,23 @@ def main():
         e2e_t.append(time.perf_counter() - t0)
         if rc != 0:
             raise RuntimeError("e2e solve failed")
-    e2e = max_over_ranks(statistics.median(e2e_t), world) / world
+    e2e = max_over_ranks(sum(e2e_t) / len(e2e_t), world) / world
     nbytes = src.nbytes
 
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and plain_iters:
         from chroma_gb300 import sources as S
         # the cost of an InvCG2 iteration does not depend on the source: time it on odd-site noise
         cpu = cpu_baseline(dims, links, S.gaussian(dims, 1, cb=1).reshape(-1, 12), int(np.median(plain_iters)), nsrc)
+
+    # the oracle's FP64 check of the solutions, and the path a factory-only Chroma input takes
+    check, factory = None, None
+    if rank == 0 and not args.no_oracle_check:
+        check, op = oracle_check(dims, links, src, psi_host)
+        if not args.no_extras:
+            factory = chroma_factory_path(ctx, G, op, src, solve_kw)
+            factory["batched_hook_e2e_s"] = e2e
+        del op
 
     extras = {} if args.no_extras else side_workloads(G)
     iters = [r["n_count"] for r in last]
@@ -496,6 +586,8 @@ def main():
         "true_rel_resid_max": max(r["rel_resid"] for r in last),
         "plain_cg_true_rel_resid_max": max(plain_res) if plain else None,
         "rel_error_vs_fp64_cg_src0": err_vs_fp64,
+        "oracle_check": check,
+        "chroma_factory_path": factory,
         "roofline": roof,
         "cpu_baseline": cpu,
         # a zero-guess full-system solve uploads only the sources (gbc_solve skips the psi upload)

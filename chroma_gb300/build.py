@@ -67,7 +67,7 @@ def build(force=False, verbose=False, jobs=None):
     newest = max(os.path.getmtime(o) for o in objs)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         cmd = [_nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC,-fopenmp", "-o", LIB + ".tmp", *objs,
-               "-lcudart", "-lgomp"]
+               "-lcudart", "-lgomp", "-ldl"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

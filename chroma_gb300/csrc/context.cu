@@ -1,4 +1,6 @@
 // C-ABI lifecycle, field import and operator application (include/gbclover.h).
+#include <dlfcn.h>
+
 #include <array>
 #include <atomic>
 #include <cmath>
@@ -168,11 +170,18 @@ void free_ctx_memory(gbc_ctx* c) {
 // epilogue, isign, reduction, nrhs and a hash of the compiled shape table; later contexts and
 // processes that find their key take the shape without timing.  The file is read once per process
 // (again if the variable changes).
+// Shipped table: tune/default.tunecache beside the library's _lib directory holds the decisions
+// for the lattices of the benchmark and the tests on GB300, read-only, consulted after
+// GBC_TUNE_CACHE and before timing (GBC_TUNE_DEFAULTS=0 ignores it).  Different shapes sum the
+// stencil's FP32 arithmetic in different orders, so a fixed table is what makes two processes give
+// bitwise-identical solves: timing alone can pick different shapes from run to run.
 namespace {
 struct TuneCache {
   std::mutex m;
   std::string path;  // file the entries were read from
   std::map<std::string, std::array<int, 4>> entries;
+  bool defaults_read = false;
+  std::map<std::string, std::array<int, 4>> defaults;  // the shipped table (never written)
 };
 TuneCache& tune_cache() {
   static TuneCache tc;
@@ -206,16 +215,28 @@ std::string tune_key(gbc_ctx* c, int prec, int recon, int mode, bool dag, int re
            nrhs, shape_table_hash());
   return buf;
 }
-void read_tune_cache(TuneCache& tc, const char* path) {
-  tc.entries.clear();
-  tc.path = path;
+void read_entries(std::map<std::string, std::array<int, 4>>& out, const char* path) {
+  out.clear();
   FILE* f = fopen(path, "r");
   if (!f) return;
   char line[512], key[400];
   int tx, nrb, minb, pair;
   while (fgets(line, sizeof line, f))
-    if (sscanf(line, "%399s %d %d %d %d", key, &tx, &nrb, &minb, &pair) == 5) tc.entries[key] = {tx, nrb, minb, pair};
+    if (sscanf(line, "%399s %d %d %d %d", key, &tx, &nrb, &minb, &pair) == 5) out[key] = {tx, nrb, minb, pair};
   fclose(f);
+}
+void read_tune_cache(TuneCache& tc, const char* path) {
+  tc.path = path;
+  read_entries(tc.entries, path);
+}
+// tune/default.tunecache relative to the directory of this shared library
+std::string default_tune_path() {
+  Dl_info info;
+  if (!dladdr(reinterpret_cast<void*>(&gbc_tune_report), &info) || !info.dli_fname) return "";
+  std::string p = info.dli_fname;
+  const size_t slash = p.rfind('/');
+  const std::string dir = slash == std::string::npos ? std::string(".") : p.substr(0, slash);
+  return dir + "/../tune/default.tunecache";
 }
 }  // namespace
 
@@ -242,22 +263,44 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, int reduce,
   }
   const char* cpath = getenv("GBC_TUNE_CACHE");
   const bool cached = c->autotune && cpath && *cpath;
+  const char* dflt = getenv("GBC_TUNE_DEFAULTS");
+  const bool use_defaults = c->autotune && !(dflt && dflt[0] == '0');
   std::string ckey;
-  if (cached) {
+  if (cached || use_defaults) {
     ckey = tune_key(c, prec, recon, mode, dag, reduce, h.nrhs);
     TuneCache& tc = tune_cache();
     std::lock_guard<std::mutex> lk(tc.m);
-    if (tc.path != cpath) read_tune_cache(tc, cpath);
-    auto e = tc.entries.find(ckey);
-    if (e != tc.entries.end()) {
-      const std::array<int, 4>& t = e->second;
+    if (cached && tc.path != cpath) read_tune_cache(tc, cpath);
+    if (use_defaults && !tc.defaults_read) {
+      const std::string dp = default_tune_path();
+      if (!dp.empty()) read_entries(tc.defaults, dp.c_str());
+      tc.defaults_read = true;
+    }
+    const std::array<int, 4>* found = nullptr;
+    const char* origin = "";
+    if (cached) {
+      auto it = tc.entries.find(ckey);
+      if (it != tc.entries.end()) {
+        found = &it->second;
+        origin = "cache";
+      }
+    }
+    if (!found && use_defaults) {
+      auto it = tc.defaults.find(ckey);
+      if (it != tc.defaults.end()) {
+        found = &it->second;
+        origin = "shipped table";
+      }
+    }
+    if (found) {
+      const std::array<int, 4>& t = *found;
       for (int si = 0; si < kNumHopShapes; ++si) {
         const HopShape& sh = kHopShapes[si];
         if (sh.tx == t[0] && sh.nrb == t[1] && sh.minb == t[2] && sh.pair == t[3] &&
             hop_shape_valid(sh, prec, h.nrhs, h.g.L[3]) && hop_blocks(sh, h.g.Vh) <= h.part_stride) {
           char line[160];
-          snprintf(line, sizeof line, "prec=%d mode=%d dag=%d reduce=%d nrhs=%d -> tx=%d nrb=%d minb=%d pair=%d (cache)\n",
-                   prec, mode, dag ? 1 : 0, reduce, h.nrhs, sh.tx, sh.nrb, sh.minb, sh.pair);
+          snprintf(line, sizeof line, "prec=%d mode=%d dag=%d reduce=%d nrhs=%d -> tx=%d nrb=%d minb=%d pair=%d (%s)\n",
+                   prec, mode, dag ? 1 : 0, reduce, h.nrhs, sh.tx, sh.nrb, sh.minb, sh.pair, origin);
           c->tune_log += line;
           c->tuned[key] = si;
           return si;

@@ -12,7 +12,9 @@ Mirrors, for Python callers and for the tests, the interface that the C++ adapte
 - ``LinOpSysSolverGB300Clover``: ``__call__(psi, chi) -> SystemSolverResults_t`` solving
   M~ psi_o = chi_o on the odd sites (syssolver_linop.h, eoprec_clover_linop_w.cc:142-187);
 - ``MdagMSysSolverGB300Clover``: M~^dag M~ psi = chi (syssolver_mdagm.h:25-35);
-- ``PrecFermActQprop``: the full-lattice propagator solve (eoprec_fermact_qprop.cc:41-80).
+- ``PrecFermActQprop``: the full-lattice propagator solve (eoprec_fermact_qprop.cc:41-80);
+- ``quark_prop4``: the spin-colour sources of a propagator solved as one batch, in place of
+  quarkProp4_a's per-source loop (quarkprop4_w.cc:31-175).
 Failure handling follows syssolver_linop_clover_quda_w.h:636-643: a relative residual above
 RsdToleranceFactor * RsdTarget raises ``SolverFailure`` unless SilentFail is set, and a
 BackupSolverParam group runs the backup solver instead (Chroma's QUDA clover solver reads that
@@ -233,6 +235,43 @@ class PrecFermActQprop(_Base):
 
     def __call__(self, psi, chi):
         return self._solve(psi, chi)
+
+
+_SPIN_RANGE = {"FULL": (0, 4), "UPPER": (0, 2), "LOWER": (2, 4)}
+
+
+def quark_prop4(qprop, q_src, quark_spin_type="FULL"):
+    """The batched counterpart of Chroma's quarkProp4_a (lib/actions/ferm/qprop/quarkprop4_w.cc:31-175)
+    for a GB300 full-system solver (``PrecFermActQprop``), as chroma_plugin's quarkProp4GB300.
+
+    quarkProp4_a calls the factory solver once per spin-colour source; here the sources are
+    extracted in its order (colour outer, spin inner; PropToFerm), each scaled to unit norm as it
+    does, and solved together as one multi-right-hand-side batch, then scaled back and placed in
+    the solution propagator (FermToProp).  QUARK_SPIN_TYPE_UPPER / _LOWER solve half the spin
+    columns and fill the other half with their negated copies (quarkprop4_w.cc:120-175).
+
+    q_src: complex array (V, Ns, Ns, Nc, Nc) indexed [site, sink spin, source spin, sink colour,
+    source colour], QDP++'s prop.elem(site).elem(s1, s2).elem(c1, c2).
+    Returns (q_sol, ncg_had, per-source SystemSolverResults_t)."""
+    q_src = np.asarray(q_src, dtype=np.complex128)
+    V = q_src.shape[0]
+    start, end = _SPIN_RANGE[quark_spin_type]
+    cols = [(c, s) for c in range(3) for s in range(start, end)]
+    chi = np.ascontiguousarray(np.stack([q_src[:, :, s, :, c] for c, s in cols]).reshape(len(cols), V, 12))
+    nrm = np.sqrt(np.einsum("kvi,kvi->k", chi.conj(), chi).real)
+    fact = np.where(nrm != 0.0, 1.0 / np.where(nrm != 0.0, nrm, 1.0), 1.0)
+    chi *= fact[:, None, None]
+    psi, results = qprop(None, chi)
+    results = results if isinstance(results, list) else [results]
+    q_sol = np.zeros_like(q_src)
+    for k, (c, s) in enumerate(cols):
+        sol = (psi[k] / fact[k]).reshape(V, 4, 3)
+        q_sol[:, :, s, :, c] = sol
+        if quark_spin_type == "UPPER":
+            q_sol[:, :, s + 2, :, c] = -sol
+        elif quark_spin_type == "LOWER":
+            q_sol[:, :, s - 2, :, c] = -sol
+    return q_sol, int(sum(r.n_count for r in results)), results
 
 
 class _Factory:

@@ -73,6 +73,7 @@ struct LatticeFermion {
 struct LatticeColorMatrix {
   const ColorMatSite& elem(int site) const;
 };
+struct LatticePropagator {};
 
 class XMLReader {
  public:

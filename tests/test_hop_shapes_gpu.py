@@ -4,7 +4,8 @@ the CPU oracle: FP16 storage (5e-3 relative), 1 and 12 right-hand sides, both is
 The two-sites-per-thread fp16 kernel pairs cb sites i and i + Vh/2, i.e. (x, y, z, t) with
 (x', y, z, t + Lt/2); lattices with odd Lt/2 (4x6x4x6, 6x4x8x10) give the paired site the other
 x parity and so exercise the index arithmetic of both cases.  The two-right-hand-sides-per-thread
-kernels (shapes 12-15) run only for even nrhs: their pins apply to the 12-RHS cases."""
+kernels (shapes 12-15) run only for even nrhs, and the mixed-precision-product kernels (shapes
+16-19) only for nrhs >= their block's right-hand sides: their pins apply to the 12-RHS cases."""
 import os
 
 import numpy as np
@@ -17,7 +18,7 @@ pytestmark = pytest.mark.gpu
 
 KAPPA = 0.115
 CSW = 1.0
-NUM_SHAPES = 16  # the candidates compiled into the library (kHopShapes)
+NUM_SHAPES = 20  # the candidates compiled into the library (kHopShapes)
 
 
 def rel(a, b):
@@ -93,11 +94,12 @@ def test_pair_kernel_mixed_solve(shape):
     assert rc == 0 and res[0]["status"] == 0
 
 
-@pytest.mark.parametrize("shape", [12, 13, 14, 15])
-def test_rhs_pair_kernel_mixed_solve(shape):
-    """A 12-RHS mixed FP16/FP64 solve whose stencil (and its fused |M psi|^2 reduction) runs on one
-    of the two-right-hand-sides-per-thread shapes: every solution reaches the FP64 true residual
-    1e-10 of the oracle operator."""
+@pytest.mark.parametrize("solver", [G.SOLVER_MIXED, G.SOLVER_BICGSTAB], ids=["cgne", "bicgstab"])
+@pytest.mark.parametrize("shape", [12, 13, 14, 15, 16, 17, 18, 19])
+def test_rhs_pair_kernel_mixed_solve(shape, solver):
+    """A 12-RHS mixed FP16/FP64 solve whose stencil (and its fused |M psi|^2, or BiCGStab's (t, s),
+    (t, t), reduction) runs on one of the two-right-hand-sides-per-thread or mixed-precision-product
+    shapes: every solution reaches the FP64 true residual 1e-10 of the oracle operator."""
     from oracle import Oracle, OracleOp
     from oracle import oracle as O
     dims = (4, 6, 4, 6)
@@ -109,7 +111,8 @@ def test_rhs_pair_kernel_mixed_solve(shape):
     try:
         ctx = _context(dims, u, mass, shape)
         try:
-            psi, res, rc = ctx.solve(chi, solver=G.SOLVER_MIXED, rsd_target=1e-10)
+            psi, res, rc = ctx.solve(chi, solver=solver, rsd_target=1e-10, delta=0.01 if solver == G.SOLVER_BICGSTAB
+                                     else 0.1)
         finally:
             ctx.close()
     finally:

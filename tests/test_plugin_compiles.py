@@ -16,7 +16,8 @@ FLAGS = ["-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
 pytestmark = pytest.mark.skipif(CXX is None, reason="no C++ compiler")
 
 
-@pytest.mark.parametrize("src", ["syssolver_gb300_clover_params.cc", "syssolver_linop_clover_gb300_w.cc"])
+@pytest.mark.parametrize("src", ["syssolver_gb300_clover_params.cc", "syssolver_linop_clover_gb300_w.cc",
+                                 "quarkprop4_gb300_w.cc"])
 def test_adapter_compiles(src):
     r = subprocess.run([CXX, *FLAGS, os.path.join(ROOT, "chroma_plugin", src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr

@@ -186,3 +186,33 @@ def test_multi_rhs_results(fake):
     psi, rs = s(None, _chi(12))
     assert psi.shape == (12, V, 12) and len(rs) == 12 and all(r.status == 0 for r in rs)
 
+
+
+def _propagator_source(seed=3):
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=(V, 4, 4, 3, 3)) + 1j * rng.normal(size=(V, 4, 4, 3, 3))
+
+
+@pytest.mark.parametrize("spin_type,solved", [("FULL", (0, 1, 2, 3)), ("UPPER", (0, 1)), ("LOWER", (2, 3))])
+def test_quark_prop4_batches_the_sources(fake, spin_type, solved):
+    """quarkProp4_a's per-source loop becomes one device call with every spin-colour source;
+    the sources are normalised like quarkProp4_a's and the solutions scaled back and placed by
+    (spin, colour), with UPPER / LOWER filling the other columns by negated copies."""
+    qprop = SS.PrecFermActQprop(np.zeros((V, 4, 3, 3), complex), DIMS,
+                                SS.SysSolverGB300CloverParams.from_xml(XML.format(silent="", backup="")))
+    q_src = _propagator_source()
+    q_sol, ncg, results = SS.quark_prop4(qprop, q_src, spin_type)
+    ctx = FakeContext.instances[-1]
+    assert len(ctx.solves) == 1  # one batched call, not one per source
+    assert ctx.solves[0]["system"] == G.SYS_FULL
+    n = 3 * len(solved)
+    assert len(results) == n and ncg == sum(r.n_count for r in results)
+    # the scripted solve returns psi = 1 for the unit-norm source: the solution is |chi| everywhere
+    for c in range(3):
+        for s in solved:
+            nrm = np.linalg.norm(q_src[:, :, s, :, c])
+            assert np.allclose(q_sol[:, :, s, :, c], nrm)
+    for c in range(3):
+        for s in set(range(4)) - set(solved):
+            other = s - 2 if spin_type == "UPPER" else s + 2
+            assert np.allclose(q_sol[:, :, s, :, c], -q_sol[:, :, other, :, c])
