@@ -27,7 +27,6 @@ static int hop_shape(const HopArgs& a, HopShape sh, cudaStream_t s) {
   GBC_SHAPE(32, 12, 2)
 #undef GBC_SHAPE
   if constexpr (std::is_same<P, PrecH>::value) {
-    if (sh.pair == 4) return DAG ? hop_launch_mr1(RECON, MODE, REDUCE, a, sh, s) : hop_launch_mr0(RECON, MODE, REDUCE, a, sh, s);
     if (sh.pair == 3) {
       // two right-hand sides per thread: blocks of TS sites x NRB right-hand sides, TS NRB / 2 threads
       if (a.nrhs & 1) return -1;

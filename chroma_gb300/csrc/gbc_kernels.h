@@ -67,9 +67,7 @@ struct HopArgs {
 // with two sites per thread (TX threads cover 2 TX sites; fp16 storage and even Lt only);
 // pair = 2: the fp16 kernel that streams the next hops through a shared-memory ring (cp.async);
 // pair = 3: the fp16 kernel with two right-hand sides per thread (TX sites x NRB right-hand sides,
-// TX NRB / 2 threads; even nrhs only); pair = 4: the fp16 kernel with mixed-precision
-// (fp16 x fp16 -> FP32) colour products, TX = 16 or 32 sites x NRB right-hand sides, one of each
-// per thread.
+// TX NRB / 2 threads; even nrhs only).
 struct HopShape {
   int tx;
   int nrb;
@@ -80,16 +78,14 @@ struct HopShape {
 constexpr HopShape kHopShapes[] = {{128, 1, 1, 0}, {128, 1, 6, 0}, {32, 4, 1, 0},  {32, 4, 5, 0},
                                    {64, 2, 4, 0},  {32, 12, 2, 0}, {128, 1, 2, 1}, {128, 1, 3, 1},
                                    {64, 1, 6, 1},  {128, 1, 3, 2}, {128, 1, 4, 2}, {64, 1, 8, 2},
-                                   {32, 12, 2, 3}, {16, 12, 5, 3}, {16, 12, 4, 3}, {16, 4, 10, 3},
-                                   {16, 12, 3, 4}, {32, 6, 3, 4}, {32, 12, 2, 4}, {32, 4, 5, 4}};
-constexpr int kNumHopShapes = 20;
+                                   {32, 12, 2, 3}, {16, 12, 5, 3}, {16, 12, 4, 3}, {16, 4, 10, 3}};
+constexpr int kNumHopShapes = 16;
 // whether shape sh can run the hopping term of precision prec over nrhs right-hand sides of a
 // lattice with time extent lt
 inline bool hop_shape_valid(const HopShape& sh, int prec, int nrhs, int lt) {
   if (sh.pair == 1) return prec == PREC_HALF && lt % 2 == 0;
   if (sh.pair == 2) return prec == PREC_HALF;
   if (sh.pair == 3) return prec == PREC_HALF && nrhs % 2 == 0 && sh.nrb <= nrhs;
-  if (sh.pair == 4) return prec == PREC_HALF && sh.nrb <= nrhs;
   return !(sh.nrb > 1 && sh.nrb > nrhs);  // a block would be mostly idle
 }
 
@@ -104,9 +100,6 @@ inline int hop_blocks(const HopShape& sh, int Vh) {
 int hop_launch_d(int recon, int mode, bool dag, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
 int hop_launch_s(int recon, int mode, bool dag, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
 int hop_launch_h(int recon, int mode, bool dag, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
-// the pair = 4 shapes (dslash_mr{0,1}.cu: isign PLUS, MINUS)
-int hop_launch_mr0(int recon, int mode, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
-int hop_launch_mr1(int recon, int mode, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
 
 // One launch over several lattices: args[l] in device memory, work[b] = (lattice, 128-site block).
 int hop_multi_launch_d(int recon, int mode, bool dag, int reduce, const HopArgs* args, const int2* work, int nwork,
