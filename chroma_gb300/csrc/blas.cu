@@ -205,6 +205,75 @@ struct XmyNormF {
   }
 };
 
+// y = x - y + tw i gamma_5 x;  acc = |y|^2   (the last step of the symmetric operator with a
+// twisted-mass term; gamma_5 = diag(1, 1, -1, -1) in the DeGrand-Rossi basis)
+template <typename P>
+struct XmyTwistNormF {
+  using Acc = typename P::real;
+  Spinor x, y;
+  double tw;
+  __device__ void operator()(int idx, int r, Acc* acc) const {
+    using T = typename P::real;
+    cplx<T> xs[12], ys[12];
+    ld<P>(xs, x, idx, r);
+    ld<P>(ys, y, idx, r);
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      const T t5 = (T)(k < 6 ? tw : -tw);
+      ys[k] = xs[k] - ys[k] + t5 * timesI(xs[k]);
+      s = fmadd(ys[k].re, ys[k].re, fmadd(ys[k].im, ys[k].im, s));
+    }
+    st<P>(y, idx, r, ys);
+    acc[0] += s;
+  }
+};
+
+// y += sigma_r x;  acc = Re <x, y>   (the shifted normal operator of the multi-shift refinement:
+// y = M~^dag M~ x on entry, (M~^dag M~ + sigma) x and x^dag (M~^dag M~ + sigma) x on exit)
+template <typename P>
+struct ShiftDotF {
+  using Acc = typename P::real;
+  const double* sigma;
+  Spinor x, y;
+  __device__ void operator()(int idx, int r, Acc* acc) const {
+    using T = typename P::real;
+    cplx<T> xs[12], ys[12];
+    ld<P>(xs, x, idx, r);
+    ld<P>(ys, y, idx, r);
+    const T sg = (T)sigma[r];
+    T d = 0;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      ys[k].re = fmadd(sg, xs[k].re, ys[k].re);
+      ys[k].im = fmadd(sg, xs[k].im, ys[k].im);
+      d = fmadd(xs[k].re, ys[k].re, fmadd(xs[k].im, ys[k].im, d));
+    }
+    st<P>(y, idx, r, ys);
+    acc[0] += d;
+  }
+};
+
+// y += sigma_r x
+template <typename P>
+struct ShiftAxpyF {
+  const double* sigma;
+  Spinor x, y;
+  __device__ void operator()(int idx, int r, double*) const {
+    using T = typename P::real;
+    cplx<T> xs[12], ys[12];
+    ld<P>(xs, x, idx, r);
+    ld<P>(ys, y, idx, r);
+    const T sg = (T)sigma[r];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      ys[k].re = fmadd(sg, xs[k].re, ys[k].re);
+      ys[k].im = fmadd(sg, xs[k].im, ys[k].im);
+    }
+    st<P>(y, idx, r, ys);
+  }
+};
+
 // x += y  (x in PX, y in PY)
 template <typename PX, typename PY>
 struct XpyF {
@@ -333,6 +402,17 @@ void blas_xpay(const Geom& g, const Spinor& r, const double* b, const Spinor& p,
 }
 void blas_xmy_norm2(const Geom& g, const Spinor& x, const Spinor& y, const Red& red, cudaStream_t s) {
   GBC_DISPATCH1(x.prec, (run<1>(g, x.nrhs, XmyNormF<PA>{x, y}, &red, s)));
+}
+void blas_xmy_twist_norm2(const Geom& g, const Spinor& x, const Spinor& y, double tw, const Red& red,
+                          cudaStream_t s) {
+  GBC_DISPATCH1(x.prec, (run<1>(g, x.nrhs, XmyTwistNormF<PA>{x, y, tw}, &red, s)));
+}
+void blas_shift_dot(const Geom& g, const double* sigma, const Spinor& x, const Spinor& y, const Red& red,
+                    cudaStream_t s) {
+  GBC_DISPATCH1(x.prec, (run<1>(g, x.nrhs, ShiftDotF<PA>{sigma, x, y}, &red, s)));
+}
+void blas_shift_axpy(const Geom& g, const double* sigma, const Spinor& x, const Spinor& y, cudaStream_t s) {
+  GBC_DISPATCH1(x.prec, (run<0>(g, x.nrhs, ShiftAxpyF<PA>{sigma, x, y}, nullptr, s)));
 }
 void blas_xpy(const Geom& g, const Spinor& x, const Spinor& y, cudaStream_t s) {
   GBC_DISPATCH2(x.prec, y.prec, (run<0>(g, x.nrhs, XpyF<PA, PB>{x, y}, nullptr, s)));

@@ -134,6 +134,65 @@ __device__ void gather_tile(__nv_bfloat16* G, const int (*nbr)[9], int V, const 
     }
 }
 
+// The block's transports staged once: lk[s][d - 1][3 a + k] = M_d[a][k] with M_{+mu} = U_mu(x) and
+// M_{-mu} = U_mu(x - mu)^dag, for every direction d = 1..8 of the SITES sites.  The forward layer
+// reads them for every right-hand side of the batch instead of reloading the link per channel.
+__device__ void stage_transports(float2 (*lk)[8][9], const int (*nbr)[9], int V, const float2* links, int site0) {
+  for (int p = threadIdx.x; p < SITES * 8 * 9; p += blockDim.x) {
+    const int e = p % 9, sd = p / 9, s = sd / 8, d = sd % 8 + 1;
+    const int j = site0 + s;
+    if (j >= V) continue;
+    const int mu = (d - 1) >> 1;
+    const bool bwd = ((d - 1) & 1) != 0;
+    const int a = e / 3, k = e % 3;
+    const float2* L = links + ((size_t)(bwd ? nbr[s][d] : j) * 4 + mu) * 9;
+    const float2 u = bwd ? L[3 * k + a] : L[3 * a + k];
+    lk[s][d - 1][e] = bwd ? make_float2(u.x, -u.y) : u;
+  }
+}
+
+// G as gather_tile, from staged transports: one task per (site, direction, channel), channel
+// fastest, so that consecutive threads read consecutive channel vectors of a neighbour and write
+// consecutive words of a row; the transport comes from shared memory instead of the links.
+template <int CIN>
+__device__ void gather_tile_staged(__nv_bfloat16* G, const int (*nbr)[9], const float2 (*lk)[8][9], int V,
+                                   const float2* h, int site0) {
+  constexpr int GP = gpitch(CIN);
+  constexpr int RW = GP / 2;  // pitch in 32-bit words
+  for (int p = threadIdx.x; p < SITES * 9 * CIN; p += blockDim.x) {
+    const int i = p % CIN, sd = p / CIN, s = sd % SITES, d = sd / SITES;
+    const int j = site0 + s;
+    uint32_t* row = reinterpret_cast<uint32_t*>(G + (size_t)(s * 3) * GP + (d * CIN + i) * 2);
+    if (j >= V) {
+      row[0] = row[RW] = row[2 * RW] = 0u;
+      continue;
+    }
+    const float2* src = h + ((size_t)nbr[s][d] * CIN + i) * 3;
+    const float2 x0 = src[0], x1 = src[1], x2 = src[2];
+    if (d == 0) {
+      row[0] = bf16x2(x0.x, x0.y);
+      row[RW] = bf16x2(x1.x, x1.y);
+      row[2 * RW] = bf16x2(x2.x, x2.y);
+      continue;
+    }
+    const float2* m = lk[s][d - 1];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float2 u0 = m[3 * a], u1 = m[3 * a + 1], u2 = m[3 * a + 2];
+      const float re = u0.x * x0.x - u0.y * x0.y + u1.x * x1.x - u1.y * x1.y + u2.x * x2.x - u2.y * x2.y;
+      const float im = u0.x * x0.y + u0.y * x0.x + u1.x * x1.y + u1.y * x1.x + u2.x * x2.y + u2.y * x2.x;
+      row[a * RW] = bf16x2(re, im);
+    }
+  }
+  // zero the K padding
+  constexpr int K = 9 * CIN * 2, KP = kpad(CIN);
+  if (KP > K)
+    for (int p = threadIdx.x; p < ROWS * (KP - K); p += blockDim.x) {
+      const int r = p / (KP - K), k = K + p % (KP - K);
+      G[(size_t)r * GP + k] = __float2bfloat16(0.f);
+    }
+}
+
 __device__ __forceinline__ uint32_t ld_bf16x2(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi) {
   return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
@@ -147,46 +206,50 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// out[b][j][o][a] = (G W^T)[row][2o + re/im]
+// out[b][j][o][a] = (G W^T)[row][2o + re/im] for every right-hand side b of the batch: the
+// weights and the block's transports are staged once, then per b the gathered tile G and its GEMM
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, const float2* links, const float2* hin,
+__global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, int batch, const float2* links, const float2* hin,
                                                    float2* hout, const __nv_bfloat16* Wr) {
   constexpr int KP = kpad(CIN), NP = npad(COUT), GP = gpitch(CIN);
   extern __shared__ __align__(16) unsigned char smem[];
   __nv_bfloat16* G = reinterpret_cast<__nv_bfloat16*>(smem);
   __nv_bfloat16* W = G + ROWS * GP;  // same pitch: the B fragment loads are conflict-free too
+  float2(*lk)[8][9] = reinterpret_cast<float2(*)[8][9]>(W + NP * GP);
   __shared__ int nbr[SITES][9];
-  const int b = blockIdx.y;
   const int site0 = blockIdx.x * SITES;
-  const float2* h = hin + (size_t)b * V * CIN * 3;
   for (int p = threadIdx.x; p < NP * KP; p += blockDim.x) W[(p / KP) * GP + p % KP] = Wr[p];
   tile_neighbours(nbr, g, V, site0);
   __syncthreads();
-  gather_tile<CIN>(G, nbr, V, links, h, site0);
-  __syncthreads();
+  stage_transports(lk, nbr, V, links, site0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gid = lane >> 2, tig = lane & 3;
   constexpr int MT = ROWS / 16, NT = NP / 8;
-  float2* out = hout + (size_t)b * V * COUT * 3;
-  for (int t = warp; t < MT * NT; t += CT / 32) {
-    const int mt = t % MT, nt = t / MT;
-    float c[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int ks = 0; ks < KP / 16; ++ks) {
-      const __nv_bfloat16* A0 = G + (size_t)(mt * 16 + gid) * GP + ks * 16 + 2 * tig;
-      const __nv_bfloat16* A1 = A0 + 8 * GP;
-      uint32_t a[4] = {ld_bf16x2(A0), ld_bf16x2(A1), ld_bf16x2(A0 + 8), ld_bf16x2(A1 + 8)};
-      const __nv_bfloat16* B0 = W + (size_t)(nt * 8 + gid) * GP + ks * 16 + 2 * tig;
-      uint32_t bb[2] = {ld_bf16x2(B0), ld_bf16x2(B0 + 8)};
-      mma_bf16(c, a, bb);
-    }
-    const int o = nt * 4 + tig;
-    if (o < COUT) {
+  for (int b = 0; b < batch; ++b) {
+    __syncthreads();  // transports staged; the previous right-hand side's GEMM is done with G
+    gather_tile_staged<CIN>(G, nbr, lk, V, hin + (size_t)b * V * CIN * 3, site0);
+    __syncthreads();
+    float2* out = hout + (size_t)b * V * COUT * 3;
+    for (int t = warp; t < MT * NT; t += CT / 32) {
+      const int mt = t % MT, nt = t / MT;
+      float c[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int ks = 0; ks < KP / 16; ++ks) {
+        const __nv_bfloat16* A0 = G + (size_t)(mt * 16 + gid) * GP + ks * 16 + 2 * tig;
+        const __nv_bfloat16* A1 = A0 + 8 * GP;
+        uint32_t a[4] = {ld_bf16x2(A0), ld_bf16x2(A1), ld_bf16x2(A0 + 8), ld_bf16x2(A1 + 8)};
+        const __nv_bfloat16* B0 = W + (size_t)(nt * 8 + gid) * GP + ks * 16 + 2 * tig;
+        uint32_t bb[2] = {ld_bf16x2(B0), ld_bf16x2(B0 + 8)};
+        mma_bf16(c, a, bb);
+      }
+      const int o = nt * 4 + tig;
+      if (o < COUT) {
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        const int row = mt * 16 + gid + 8 * half;
-        const int s = row / 3, a = row % 3;
-        const int j = site0 + s;
-        if (j < V) out[((size_t)j * COUT + o) * 3 + a] = make_float2(c[2 * half], c[2 * half + 1]);
+        for (int half = 0; half < 2; ++half) {
+          const int row = mt * 16 + gid + 8 * half;
+          const int s = row / 3, a = row % 3;
+          const int j = site0 + s;
+          if (j < V) out[((size_t)j * COUT + o) * 3 + a] = make_float2(c[2 * half], c[2 * half + 1]);
+        }
       }
     }
   }
@@ -347,14 +410,16 @@ __global__ void links_kernel(Geom g, int V, const double2* canon, float2* links)
 template <int CIN, int COUT>
 void launch_layer(const Geom& g, int V, int batch, const float2* links, const float2* in, float2* out,
                   const __nv_bfloat16* W, cudaStream_t s) {
-  const size_t smem = (size_t)(ROWS * gpitch(CIN) + npad(COUT) * gpitch(CIN)) * 2;
+  // tile G and weights W (bf16 at pitch gpitch; their bytes are a multiple of 8), then the staged
+  // transports (float2)
+  const size_t smem = (size_t)(ROWS * gpitch(CIN) + npad(COUT) * gpitch(CIN)) * 2 + sizeof(float2) * SITES * 8 * 9;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(layer_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  dim3 grid((V + SITES - 1) / SITES, batch);
-  layer_kernel<CIN, COUT><<<grid, CT, smem, s>>>(g, V, links, in, out, W);
+  dim3 grid((V + SITES - 1) / SITES);
+  layer_kernel<CIN, COUT><<<grid, CT, smem, s>>>(g, V, batch, links, in, out, W);
   count_launch();
 }
 

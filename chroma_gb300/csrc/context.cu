@@ -422,7 +422,9 @@ void ensure_sym(gbc_ctx* c, int prec) {
 // Symmetric even-odd operator (seoprec_clover_linop_w.cc:145-187):
 //   PLUS   out = in - 1/4 A_oo^-1 D_oe A_ee^-1 D_eo in     (t_e, then the clover-inverse epilogue)
 //   MINUS  out = in - 1/4 D_oe^dag A_ee^-1 D_eo^dag A_oo^-1 in
-// The last step leaves 1/4 (...) in out and blas_xmy_norm2 turns it into in - out with |out|^2.
+// The last step leaves 1/4 (...) in out and blas_xmy_norm2 turns it into in - out with |out|^2;
+// with a twisted-mass term, in - out + isign i mu gamma_5 in (seoprec_clover_linop_w.cc:174-184:
+// the clover term and its inverses carry no twist, the term is added to M_s itself).
 void apply_seo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e,
                int reduce) {
   ensure_sym(c, prec);
@@ -436,7 +438,10 @@ void apply_seo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& o
     hop(c, prec, 0, HOP_CLOV, true, 1.0, to, tmp_e, nullptr, f.clovinv, false);
     hop(c, prec, 1, HOP_PLAIN, true, 0.25, tmp_e, out, nullptr, nullptr, false);
   }
-  blas_xmy_norm2(c->g, in, out, red(c), c->stream);
+  if (c->act.twisted && c->act.twisted_m != 0.0)
+    blas_xmy_twist_norm2(c->g, in, out, dag ? -c->act.twisted_m : c->act.twisted_m, red(c), c->stream);
+  else
+    blas_xmy_norm2(c->g, in, out, red(c), c->stream);
   (void)reduce;
 }
 
@@ -677,8 +682,6 @@ int gbc_apply(gbc_ctx* c, int op, int isign, int cb, int prec, int nrhs, double*
   if (prec != GBC_PREC_DOUBLE && prec != GBC_PREC_SINGLE && prec != GBC_PREC_HALF) return GBC_ERR_ARGS;
   if (!c->have_gauge) return fail(c, GBC_ERR_STATE, "load the gauge field first");
   if (op < 0 || op > 7 || cb < 0 || cb > 1) return GBC_ERR_ARGS;
-  if ((op == GBC_OP_SYM || op == GBC_OP_SYM_MDAGM) && c->act.twisted)
-    return fail(c, GBC_ERR_ARGS, "the symmetric operator is not built with a twisted-mass term");
   return guarded(c, [&]() {
     ensure_prec(c, prec);
     ensure_stage(c, nrhs);

@@ -149,6 +149,9 @@ int noalloc_reserve();
 void precond_free(gbc_ctx* c);
 // out ~= M~^-1 in (odd checkerboard fields, same precision, nrhs right-hand sides)
 void precond_apply(gbc_ctx* c, const Spinor& in, const Spinor& out);
+// layers of the loaded network and the channels of layer l (its output side when out)
+int precond_layers(gbc_ctx* c);
+int precond_channels(gbc_ctx* c, int l, bool out);
 
 // ---- inner BiCGStab (bicgstab.cu) ----------------------------------------------------------------
 struct InnerStats {
@@ -168,6 +171,13 @@ void bicgstab_xr_update(gbc_ctx* c, int pa, int po, const double* alpha_omega, i
                         const Spinor& r, const Spinor& p, const Spinor& v, const Spinor& t, const Spinor& r0);
 
 // ---- solvers (solvers.cu) -------------------------------------------------------------------
+// FP64 defect correction of the shifted normal systems (M~^dag M~ + sigma_q) psi_q = chi, one per
+// right-hand side q of psi (FP64, holding the initial guesses), the corrections from CG with
+// per-right-hand-side shifts d_shift (device) in the sloppy operator precision; returns the CG
+// iterations per shift, the final FP64 |chi - (M~^dag M~ + sigma_q) psi_q|^2 in rr and a status
+std::vector<int> refine_shifted(gbc_ctx* c, int sloppy, const Spinor& chi, const double* d_shift,
+                                const Spinor& psi, const std::vector<double>& rsd, int max_iter,
+                                std::vector<double>& rr, std::vector<int>& status);
 // after_export (optional) runs once the solution is in psi_canon on the context stream and before
 // the final residual check, which only reads it: gbc_solve starts the copy to the host there
 int solve_device(gbc_ctx* c, const gbc_solve_params* p, int nrhs, double* psi_canon, const double* chi_canon,

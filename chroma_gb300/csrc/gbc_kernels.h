@@ -176,6 +176,14 @@ void blas_cg_update(const Geom& g, const double* a, const Spinor& x, const Spino
 void blas_xpay(const Geom& g, const Spinor& r, const double* b, const Spinor& p, cudaStream_t s);
 // y = x - y, result = |y|^2    (residual from a source and M psi)
 void blas_xmy_norm2(const Geom& g, const Spinor& x, const Spinor& y, const Red& red, cudaStream_t s);
+// y = x - y + tw i gamma_5 x, result = |y|^2   (tw real, the same for every right-hand side)
+void blas_xmy_twist_norm2(const Geom& g, const Spinor& x, const Spinor& y, double tw, const Red& red,
+                          cudaStream_t s);
+// y += sigma_r x and result = Re <x, y> (x, y same precision; sigma per rhs, device)
+void blas_shift_dot(const Geom& g, const double* sigma, const Spinor& x, const Spinor& y, const Red& red,
+                    cudaStream_t s);
+// y += sigma_r x (x, y same precision; sigma per rhs, device)
+void blas_shift_axpy(const Geom& g, const double* sigma, const Spinor& x, const Spinor& y, cudaStream_t s);
 // x += y (y may be lower precision)
 void blas_xpy(const Geom& g, const Spinor& x, const Spinor& y, cudaStream_t s);
 // finalize the partial sums of nred quantities x nrhs into red.result

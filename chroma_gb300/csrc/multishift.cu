@@ -1,6 +1,9 @@
 // Multi-shift CG on the normal equations, (M~^dag M~ + sigma_s) psi_s = chi for every shift at
 // once: the RHMC solver behind Chroma's MdagMMultiSysSolverCG (multi_syssolver_mdagm_cg.h:58-80)
-// -> MInvCG2 (minvcg2.cc:70-357), Jegerlehner's recursion (hep-lat/9708029).  One Krylov space of
+// -> MInvCG2 (minvcg2.cc:70-357), Jegerlehner's recursion (hep-lat/9708029).  With a sloppy
+// precision (HALF or SINGLE) the recursion runs in FP32 and each shift is then refined by an FP64
+// defect correction whose corrections come from CG on the shifted system in the sloppy operator,
+// Chroma's multiprec pattern (a single-precision MInvCG2 followed by per-shift refinement).  One Krylov space of
 // the unshifted M~^dag M~ is built; each shifted solution follows from the ratios zeta_s of its
 // residual to the unshifted one, so an iteration costs one M~^dag M~ plus one fused update of all
 // shifted search vectors and one of all solutions.  Fields and sums in FP64, the scalar recursion
@@ -62,7 +65,18 @@ int solve_multishift(gbc_ctx* c, const gbc_solve_params* pp, int ns, const doubl
   const Geom& g = c->g;
   cudaStream_t s = c->stream;
   const int max_iter = pp->max_iter > 0 ? pp->max_iter : 10000;
+  // mixed precision (sloppy_precision HALF or SINGLE): the shared-Krylov recursion runs on FP32
+  // fields and the FP32 operator to a relative 1e-6 (near FP32's floor), then every shift is
+  // refined by the FP64 defect correction of refine_shifted (batched over the shifts, corrections
+  // from CG in the sloppy operator); else the recursion runs in FP64 to the targets
+  const int sp = pp->sloppy_precision;
+  const bool mixed = sp == PREC_HALF || sp == PREC_SINGLE;
+  const int W = mixed ? PREC_SINGLE : D;
   ensure_prec(c, D);
+  if (mixed) {
+    ensure_prec(c, PREC_SINGLE);
+    ensure_prec(c, sp);
+  }
   const double t0 = now();
   cudaEvent_t ev0, ev1;
   GBC_CUDA(cudaEventCreate(&ev0));
@@ -70,18 +84,21 @@ int solve_multishift(gbc_ctx* c, const gbc_solve_params* pp, int ns, const doubl
   GBC_CUDA(cudaEventRecord(ev0, s));
   const long long launches0 = launch_count();
 
-  Spinor chi = sub(workspace(c, MS_CHI, D, 1), 0, 1);
-  Spinor r = sub(workspace(c, MS_R, D, 1), 0, 1);
-  Spinor p0 = sub(workspace(c, MS_P0, D, 1), 0, 1);
-  Spinor mp = sub(workspace(c, MS_MP, D, 1), 0, 1);
-  Spinor mmp = sub(workspace(c, MS_MMP, D, 1), 0, 1);
-  Spinor te = sub(workspace(c, MS_TE, D, 1), 0, 1);
-  Spinor P = sub(workspace(c, MS_P, D, ns), 0, ns);
-  Spinor X = sub(workspace(c, MS_X, D, ns), 0, ns);
+  const int o = 20 * pidx(W);  // workspace slots per recursion precision
+  Spinor chid = sub(workspace(c, MS_CHI, D, 1), 0, 1);
+  Spinor chi = mixed ? sub(workspace(c, MS_CHI + o, W, 1), 0, 1) : chid;
+  Spinor r = sub(workspace(c, MS_R + o, W, 1), 0, 1);
+  Spinor p0 = sub(workspace(c, MS_P0 + o, W, 1), 0, 1);
+  Spinor mp = sub(workspace(c, MS_MP + o, W, 1), 0, 1);
+  Spinor mmp = sub(workspace(c, MS_MMP + o, W, 1), 0, 1);
+  Spinor te = sub(workspace(c, MS_TE + o, W, 1), 0, 1);
+  Spinor P = sub(workspace(c, MS_P + o, W, ns), 0, ns);
+  Spinor X = sub(workspace(c, MS_X + o, W, ns), 0, ns);
   const size_t rs = (size_t)c->V * 24;
   ensure_stage(c, ns);
   GBC_CUDA(cudaMemcpyAsync(c->d_stage[0], chi_canon, rs * sizeof(double), cudaMemcpyHostToDevice, s));
-  import_spinor(g, c->d_stage[0], rs, 1, chi, s);
+  import_spinor(g, c->d_stage[0], rs, 1, chid, s);
+  if (mixed) blas_copy(g, chi, chid, s);
   Coefs co(ns), one(1);
 
   std::vector<double> shift(shifts, shifts + ns), rsd_sq(ns);
@@ -92,7 +109,10 @@ int solve_multishift(gbc_ctx* c, const gbc_solve_params* pp, int ns, const doubl
   if (!(chi2 > 0.0)) {
     status = std::isfinite(chi2) ? GBC_OK : GBC_ERR_NONFINITE;
   } else {
-    for (int q = 0; q < ns; ++q) rsd_sq[q] = chi2 * rsd[q] * rsd[q];
+    for (int q = 0; q < ns; ++q) {
+      const double t = mixed ? std::max(rsd[q], 1e-6) : rsd[q];
+      rsd_sq[q] = chi2 * t * t;
+    }
     const int smallest = (int)(std::min_element(shift.begin(), shift.end()) - shift.begin());
     // r = p0 = p_s = chi
     blas_copy(g, r, chi, s);
@@ -100,9 +120,9 @@ int solve_multishift(gbc_ctx* c, const gbc_solve_params* pp, int ns, const doubl
     blas_copy(g, P, broadcast(chi, ns), s);
     // b = -|r|^2 / <p0, A p0>,  r += b A p0
     double cp = chi2;
-    apply_meo(c, D, false, p0, mp, te, true);
+    apply_meo(c, W, false, p0, mp, te, true);
     double d = fetch(c);
-    apply_meo(c, D, true, mp, mmp, te, false);
+    apply_meo(c, W, true, mp, mmp, te, false);
     double b = -cp / d;
     one.h[0] = make_double2(b, 0.0);
     one.h[1] = make_double2(1.0, 0.0);
@@ -141,9 +161,9 @@ int solve_multishift(gbc_ctx* c, const gbc_solve_params* pp, int ns, const doubl
       }
       co.axpby(c, broadcast(r, ns), P);
       cp = cc;
-      apply_meo(c, D, false, p0, mp, te, true);
+      apply_meo(c, W, false, p0, mp, te, true);
       d = fetch(c);
-      apply_meo(c, D, true, mp, mmp, te, false);
+      apply_meo(c, W, true, mp, mmp, te, false);
       const double bp = b;
       b = -cp / d;
       one.h[0] = make_double2(b, 0.0);
@@ -173,6 +193,29 @@ int solve_multishift(gbc_ctx* c, const gbc_solve_params* pp, int ns, const doubl
     }
     if (!done && status == GBC_OK) status = GBC_ERR_NOT_CONVERGED;
   }
+  // mixed precision: FP64 copies of the solutions, refined shift by shift (batched)
+  std::vector<int> refine_iters(ns, 0), refine_status(ns, GBC_OK);
+  std::vector<double> refine_rr;
+  Spinor XD = X;
+  if (mixed) {
+    XD = sub(workspace(c, MS_X, D, ns), 0, ns);
+    blas_copy(g, XD, X, s);
+    if (status == GBC_OK || status == GBC_ERR_NOT_CONVERGED) {
+      double* d_shift = nullptr;
+      GBC_CUDA(cudaMalloc(&d_shift, sizeof(double) * ns));
+      GBC_CUDA(cudaMemcpyAsync(d_shift, shift.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, s));
+      std::vector<double> rsdv(rsd, rsd + ns);
+      try {
+        refine_iters = refine_shifted(c, sp, chid, d_shift, XD, rsdv, std::max(1, max_iter - iters), refine_rr,
+                                      refine_status);
+      } catch (...) {
+        cudaFree(d_shift);
+        throw;
+      }
+      cudaFree(d_shift);
+      status = GBC_OK;
+    }
+  }
   GBC_CUDA(cudaEventRecord(ev1, s));
   GBC_CUDA(cudaEventSynchronize(ev1));
   float ms = 0.f;
@@ -183,23 +226,25 @@ int solve_multishift(gbc_ctx* c, const gbc_solve_params* pp, int ns, const doubl
   // (the even sites of psi_s are kept: the caller's arrays are staged first)
   Spinor t1 = sub(workspace(c, MS_T1, D, 1), 0, 1);
   Spinor t2 = sub(workspace(c, MS_T2, D, 1), 0, 1);
+  Spinor ted = sub(workspace(c, MS_TE, D, 1), 0, 1);
   for (int q = 0; q < ns; ++q) {
-    Spinor xq = sub(X, q, 1);
-    apply_meo(c, D, false, xq, t1, te, false);
-    apply_meo(c, D, true, t1, t2, te, false);
+    Spinor xq = sub(XD, q, 1);
+    apply_meo(c, D, false, xq, t1, ted, false);
+    apply_meo(c, D, true, t1, t2, ted, false);
     one.h[0] = make_double2(shift[q], 0.0);
     one.h[1] = make_double2(1.0, 0.0);
     one.axpby(c, xq, t2);  // t2 = (M~^dag M~ + sigma) psi
-    blas_xmy_norm2(g, chi, t2, red(c), s);
+    blas_xmy_norm2(g, chid, t2, red(c), s);
     const double rr = fetch(c);
     gbc_result& o = res[q];
     o = gbc_result{};
-    o.n_count = iters;
+    o.n_count = iters + refine_iters[q];
+    o.n_outer = mixed ? 1 : 0;
     o.resid = std::sqrt(rr);
     o.rel_resid = chi2 > 0 ? std::sqrt(rr / chi2) : 0.0;
-    o.status = status;
-    if (status == GBC_OK && !(o.rel_resid <= pp->rsd_tolerance_factor * rsd[q])) o.status = GBC_ERR_NOT_CONVERGED;
-    if (status == GBC_ERR_NOT_CONVERGED && o.rel_resid <= pp->rsd_tolerance_factor * rsd[q]) o.status = GBC_OK;
+    o.status = mixed && status == GBC_OK ? refine_status[q] : status;
+    if (o.status == GBC_ERR_NOT_CONVERGED) o.status = GBC_OK;  // judged by the tolerance factor below
+    if (o.status == GBC_OK && !(o.rel_resid <= pp->rsd_tolerance_factor * rsd[q])) o.status = GBC_ERR_NOT_CONVERGED;
     o.device_seconds = ms * 1e-3;
     o.launches = (int)launches;
     GBC_CUDA(cudaMemcpyAsync(c->d_stage[1], psi_canon[q], rs * sizeof(double), cudaMemcpyHostToDevice, s));

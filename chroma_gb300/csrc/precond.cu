@@ -30,6 +30,9 @@ void precond_apply(gbc_ctx* c, const Spinor& in, const Spinor& out) {
   cnn_apply_spinor(c, *n, in, out);
 }
 
+int precond_layers(gbc_ctx* c) { return c->precond ? net_of(c)->nlayers : 0; }
+int precond_channels(gbc_ctx* c, int l, bool out) { return out ? net_of(c)->cout(l) : net_of(c)->cin(l); }
+
 }  // namespace gbc
 
 using namespace gbc;

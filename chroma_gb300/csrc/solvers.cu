@@ -26,6 +26,7 @@
 #include <complex>
 
 #include "ctx.h"
+#include "dense.h"
 #include "krylov.h"
 
 namespace gbc {
@@ -71,6 +72,7 @@ struct CgCfg {
   int maxit;
   double delta;      // reliable-update trigger (0: none)
   int check_every;   // host convergence checks
+  const double* shift = nullptr;  // device, per right-hand side: solve (M~^dag M~ + shift) x = b
 };
 
 struct CgStats {
@@ -100,6 +102,7 @@ CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b
     Spinor t1 = sub(workspace(c, SLOT_T1 + 100 * pidx(cfg.pa), cfg.pa, n), 0, n);
     Spinor teh = sub(workspace(c, SLOT_TEH + 100 * pidx(cfg.pa), cfg.pa, n), 0, n);
     apply_sys(c, cfg.pa, true, x, r, t1, teh);
+    if (cfg.shift) blas_shift_axpy(g, cfg.shift, x, r, s);
     blas_xmy_norm2(g, b, r, red(c), s);
   };
   if (zero_x) {
@@ -130,9 +133,17 @@ CgStats cg_normal(gbc_ctx* c, const CgCfg& cfg, const Spinor& x, const Spinor& b
   for (int i = 0; i < n; ++i) any |= hs[i].active != 0;
   // One iteration, all scalars on the device: no host round trip inside.
   auto body = [&]() {
-    apply_meo(c, cfg.po, false, p, mp, te, true);     // |mp|^2 -> result
-    cg_alpha(c->d_cg, c->d_result, c->d_a, n, s);
-    apply_meo(c, cfg.po, true, mp, mmp, te, false);
+    if (cfg.shift) {
+      // mmp = (M~^dag M~ + shift) p and p^dag mmp -> result
+      apply_meo(c, cfg.po, false, p, mp, te, false);
+      apply_meo(c, cfg.po, true, mp, mmp, te, false);
+      blas_shift_dot(g, cfg.shift, p, mmp, red(c), s);
+      cg_alpha(c->d_cg, c->d_result, c->d_a, n, s);
+    } else {
+      apply_meo(c, cfg.po, false, p, mp, te, true);     // |mp|^2 -> result
+      cg_alpha(c->d_cg, c->d_result, c->d_a, n, s);
+      apply_meo(c, cfg.po, true, mp, mmp, te, false);
+    }
     blas_cg_update(g, c->d_a, x, p, r, mmp, red(c), s);  // |r|^2 -> result
     cg_beta(c->d_cg, c->d_result, c->d_b, n, s);
     blas_xpay(g, r, c->d_b, p, s);                     // p = r + b p (b = 0 once converged)
@@ -333,12 +344,19 @@ CgStats reliable_cg(gbc_ctx* c, int po, const Spinor& psi, const Spinor& chi, do
   return st;
 }
 
-// Batched right-preconditioned FGMRES(m) on M~ x = b (FlexibleArnoldiT + Givens + LeastSquaresSolve,
-// syssolver_linop_fgmres_dr.{h:31-148, cc:77-195, 256-273, 459-765}, NDefl = 0).  Krylov vectors in
-// precision pa, operator in po; the preconditioner (learned network) maps V_j to Z_j, or Z_j = V_j.
-// Orthogonalisation: classical Gram-Schmidt applied twice (two block reductions per step instead of
-// j + 1 dependent ones).  Stops a right-hand side when |g_{j+1}| <= tol |b|.
-CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, double tol, int maxit, int m,
+// Batched right-preconditioned FGMRES-DR(m, k) on M~ x = b (FlexibleArnoldiT + Givens +
+// LeastSquaresSolve, syssolver_linop_fgmres_dr.{h:31-148, cc:77-195, 256-273, 459-765}).  Krylov
+// vectors in precision pa, operator in po; the preconditioner (learned network) maps V_j to Z_j,
+// or Z_j = V_j.  One classical Gram-Schmidt pass per Arnoldi step.  Stops a right-hand side when
+// |g_{j+1}| <= tol |b|.
+// Deflated restarts (k = ndefl > 0, Morgan's GMRES-DR in the flexible form of the reference,
+// :520-700): after a cycle of dimension d, the k harmonic Ritz vectors of smallest modulus -- here
+// the Schur vectors of H_d + f h^H, f = H_d^-H h, h^H the last row of H, which span the same
+// invariant subspace as the reference's eigenvectors -- and the cycle's least-squares residual
+// c - H eta form G_{k+1}; with its orthonormal factor Q_{k+1} the next cycle starts from
+// V' = V Q_{k+1}, Z' = Z Q_k, H' = Q_{k+1}^H H Q_k and c' = V'^H r, and its Arnoldi process extends
+// the basis from column k.  Each right-hand side keeps its own H, Q and rotations.
+CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, double tol, int maxit, int m, int kdef,
                bool use_precond, const std::vector<int>& active0) {
   using cd = std::complex<double>;
   const int n = x.nrhs;
@@ -346,14 +364,22 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
   cudaStream_t s = c->stream;
   if (m < 1) m = 1;
   if (m > kMaxKrylov - 1) m = kMaxKrylov - 1;
-  VecList V, Z;
-  for (int j = 0; j <= m; ++j) V.v[j] = sub(workspace(c, 300 + j, pa, n), 0, n);
+  kdef = std::max(0, std::min(kdef, kMaxKrylov - 1 - m));
+  const int mk = m + kdef;  // columns of a deflated cycle
+  const int ldh = mk + 1;
+  VecList V, Z, NV, NZ;
+  for (int j = 0; j <= mk; ++j) V.v[j] = sub(workspace(c, 300 + j, pa, n), 0, n);
   const bool prec = use_precond && c->precond != nullptr;
-  for (int j = 0; j < m; ++j) Z.v[j] = prec ? sub(workspace(c, 340 + j, pa, n), 0, n) : V.v[j];
+  for (int j = 0; j < mk; ++j) Z.v[j] = prec ? sub(workspace(c, 340 + j, pa, n), 0, n) : V.v[j];
   Spinor w = sub(workspace(c, 380, pa, n), 0, n);
   Spinor oin = sub(workspace(c, 381, po, n), 0, n);
   Spinor oout = sub(workspace(c, 382, po, n), 0, n);
   Spinor te = sub(workspace(c, 383, po, n), 0, n);
+  if (kdef > 0) {
+    for (int t = 0; t <= kdef; ++t) NV.v[t] = sub(workspace(c, 400 + t, pa, n), 0, n);
+    if (prec)
+      for (int t = 0; t < kdef; ++t) NZ.v[t] = sub(workspace(c, 440 + t, pa, n), 0, n);
+  }
   Red kred{c->d_kpartials, c->kpart_stride, c->d_kresult};
   CgStats st;
   st.iters.assign(n, 0);
@@ -374,9 +400,25 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
     for (size_t k = 0; k < cf.size(); ++k) c->h_kcoef[k] = make_double2(cf[k].real(), cf[k].imag());
     GBC_CUDA(cudaMemcpyAsync(c->d_kcoef, c->h_kcoef, sizeof(double2) * rows * n, cudaMemcpyHostToDevice, s));
   };
+  auto fetch_dots = [&](int rows) {  // the rows of a multi_cdot, [row * n + rhs]
+    GBC_CUDA(cudaMemcpyAsync(c->h_kresult, c->d_kresult, sizeof(double) * 2 * rows * n, cudaMemcpyDeviceToHost, s));
+    sync(c);
+    std::vector<cd> out((size_t)rows * n);
+    for (int q = 0; q < rows; ++q)
+      for (int i = 0; i < n; ++i)
+        out[q * n + i] = cd(c->h_kresult[(q * 2 + 0) * n + i], c->h_kresult[(q * 2 + 1) * n + i]);
+    return out;
+  };
   int total = 0;
   Spinor tea = sub(workspace(c, 384, pa, n), 0, n);
   std::vector<double> prev_beta(n, HUGE_VAL);
+  // kept from one cycle to the next for the deflated restart: the unrotated H (column-major,
+  // ldh rows), the right-hand side c of the cycle's least-squares problem, its solution eta and
+  // the cycle's dimension
+  std::vector<std::vector<cd>> H(n, std::vector<cd>((size_t)ldh * mk, 0.0)), cvec(n, std::vector<cd>(ldh, 0.0));
+  std::vector<std::vector<cd>> eta_prev(n);
+  std::vector<int> prev_dim(n, 0);
+  int cycle = 0;
   while (total < maxit) {
     // r = b - A x with the operator in the vectors' precision: each restart is a refinement step,
     // so the cycles may run on the cheaper sloppy operator
@@ -398,17 +440,144 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
       all &= done[i] != 0;
     }
     if (all) break;
-    std::vector<cd> a(n);
-    for (int i = 0; i < n; ++i) a[i] = done[i] ? 0.0 : 1.0 / beta[i];
-    put_coef(a, 1);
-    blas_cax(g, c->d_kcoef, w, V.v[0], s);
-    // per right-hand side: R (column-major, R[col][row]), g, Givens (c, s)
-    std::vector<std::vector<cd>> R(n, std::vector<cd>((m + 1) * m, 0.0)), gv(n, std::vector<cd>(m + 1, 0.0));
-    std::vector<std::vector<cd>> gc(n, std::vector<cd>(m)), gs(n, std::vector<cd>(m));
-    std::vector<int> dim(n, 0), cyc_done(done);
-    for (int i = 0; i < n; ++i) gv[i][0] = beta[i];
+    // a deflated restart needs a previous cycle longer than the deflation space on every
+    // right-hand side still running
+    bool deflate = kdef > 0 && cycle > 0;
+    for (int i = 0; i < n && deflate; ++i)
+      if (!done[i] && prev_dim[i] <= kdef) deflate = false;
+    const int kc = deflate ? kdef : 0;
+    // per right-hand side: R (column-major, R[col][row]), g, the Givens rotations of the cycle's
+    // columns (c, s), and for a deflated cycle the rotations (row pairs) that triangularised H'
+    std::vector<std::vector<cd>> R(n, std::vector<cd>((size_t)ldh * mk, 0.0)), gv(n, std::vector<cd>(ldh, 0.0));
+    std::vector<std::vector<cd>> gc(n, std::vector<cd>(mk)), gs(n, std::vector<cd>(mk));
+    std::vector<std::vector<int>> qrow(n);
+    std::vector<std::vector<cd>> qc(n), qs(n);
+    std::vector<int> dim(n, kc), cyc_done(done);
+    // rotation (A, B) -> (conj(c) A + conj(s) B, -s A + c B) on rows (r, r + 1) of a vector
+    auto rot = [](std::vector<cd>& v, int r, cd cc, cd ss, size_t off) {
+      const cd A = v[off + r], B = v[off + r + 1];
+      v[off + r] = std::conj(cc) * A + std::conj(ss) * B;
+      v[off + r + 1] = -ss * A + cc * B;
+    };
+    auto givens = [](cd f, cd gg, cd& cc, cd& ss) -> cd {  // syssolver_linop_fgmres_dr.h:31-148
+      if (f == 0.0) {
+        cc = 0.0;
+        ss = 1.0;
+        return gg;
+      }
+      if (gg == 0.0) {
+        ss = 0.0;
+        cc = std::conj(f) / std::abs(f);
+        return std::abs(f);
+      }
+      const double t = std::sqrt(std::norm(f) + std::norm(gg));
+      cc = f / t;
+      ss = gg / t;
+      return t;
+    };
+    if (!deflate) {
+      std::vector<cd> a(n);
+      for (int i = 0; i < n; ++i) a[i] = done[i] ? 0.0 : 1.0 / beta[i];
+      put_coef(a, 1);
+      blas_cax(g, c->d_kcoef, w, V.v[0], s);
+      for (int i = 0; i < n; ++i) {
+        std::fill(H[i].begin(), H[i].end(), cd(0.0));
+        std::fill(cvec[i].begin(), cvec[i].end(), cd(0.0));
+        gv[i][0] = cvec[i][0] = beta[i];
+      }
+    } else {
+      // Q_{k+1} per right-hand side (column-major, (d + 1) x (k + 1)) and H' = Q_{k+1}^H H Q_k
+      std::vector<std::vector<cd>> Qk(n), Hn(n);
+      int dmax = 0;
+      for (int i = 0; i < n; ++i) {
+        if (done[i]) continue;
+        const int d = prev_dim[i];
+        dmax = std::max(dmax, d);
+        std::vector<cd> Hd((size_t)d * d), f(d);
+        for (int col = 0; col < d; ++col) {
+          for (int row = 0; row < d; ++row) Hd[(size_t)col * d + row] = H[i][(size_t)col * ldh + row];
+          f[col] = std::conj(H[i][(size_t)col * ldh + d]);  // h = (last row of H)^H
+        }
+        std::vector<cd> Am = Hd, Y;
+        if (!dense::lu_solve(d, Hd, f, true)) throw std::string("FGMRES-DR: singular Hessenberg block");
+        for (int col = 0; col < d; ++col)
+          for (int row = 0; row < d; ++row) Am[(size_t)col * d + row] += f[row] * H[i][(size_t)col * ldh + d];
+        if (!dense::schur(d, Am, Y)) throw std::string("FGMRES-DR: harmonic Ritz values did not converge");
+        dense::sort_smallest(d, Am, Y, kc);
+        std::vector<cd> G((size_t)(d + 1) * (kc + 1), 0.0), Rg;
+        for (int col = 0; col < kc; ++col)
+          for (int row = 0; row < d; ++row) G[(size_t)col * (d + 1) + row] = Y[(size_t)col * d + row];
+        for (int row = 0; row <= d; ++row) {
+          cd v = cvec[i][row];
+          for (int col = 0; col < d; ++col) v -= H[i][(size_t)col * ldh + row] * eta_prev[i][col];
+          G[(size_t)kc * (d + 1) + row] = v;
+        }
+        dense::qr_thin(d + 1, kc + 1, G, Rg);
+        // H Q_k ((d + 1) x k), then Q_{k+1}^H (H Q_k)
+        std::vector<cd> HQ((size_t)(d + 1) * kc, 0.0);
+        for (int col = 0; col < kc; ++col)
+          for (int row = 0; row <= d; ++row) {
+            cd v = 0.0;
+            for (int q = 0; q < d; ++q) v += H[i][(size_t)q * ldh + row] * G[(size_t)col * (d + 1) + q];
+            HQ[(size_t)col * (d + 1) + row] = v;
+          }
+        Hn[i].assign((size_t)(kc + 1) * kc, 0.0);
+        for (int col = 0; col < kc; ++col)
+          for (int row = 0; row <= kc; ++row) {
+            cd v = 0.0;
+            for (int q = 0; q <= d; ++q) v += std::conj(G[(size_t)row * (d + 1) + q]) * HQ[(size_t)col * (d + 1) + q];
+            Hn[i][(size_t)col * (kc + 1) + row] = v;
+          }
+        Qk[i] = G;
+      }
+      // the new basis: V'_t = sum_j V_j Q(j, t), Z'_t = sum_j Z_j Q(j, t) (per right-hand side)
+      for (int t = 0; t <= kc; ++t) {
+        std::vector<cd> cf((size_t)(dmax + 1) * n, 0.0);
+        for (int i = 0; i < n; ++i)
+          if (!done[i])
+            for (int j = 0; j <= prev_dim[i]; ++j) cf[(size_t)j * n + i] = Qk[i][(size_t)t * (prev_dim[i] + 1) + j];
+        put_coef(cf, dmax + 1);
+        blas_zero(g, NV.v[t], s);
+        multi_caxpy(g, V, dmax + 1, c->d_kcoef, NV.v[t], 1.0, s);
+        if (prec && t < kc) {
+          blas_zero(g, NZ.v[t], s);
+          multi_caxpy(g, Z, dmax, c->d_kcoef, NZ.v[t], 1.0, s);
+        }
+      }
+      for (int t = 0; t <= kc; ++t) blas_copy(g, V.v[t], NV.v[t], s);
+      if (prec)
+        for (int t = 0; t < kc; ++t) blas_copy(g, Z.v[t], NZ.v[t], s);
+      // c' = V'^H r
+      multi_cdot(g, V, kc + 1, w, kred, s);
+      std::vector<cd> cn = fetch_dots(kc + 1);
+      for (int i = 0; i < n; ++i) {
+        std::fill(H[i].begin(), H[i].end(), cd(0.0));
+        std::fill(cvec[i].begin(), cvec[i].end(), cd(0.0));
+        if (done[i]) continue;
+        for (int col = 0; col < kc; ++col)
+          for (int row = 0; row <= kc; ++row) H[i][(size_t)col * ldh + row] = Hn[i][(size_t)col * (kc + 1) + row];
+        for (int row = 0; row <= kc; ++row) cvec[i][row] = gv[i][row] = cn[(size_t)row * n + i];
+        // triangularise H' (full, (k + 1) x k) by rotations of adjacent rows, bottom up per column;
+        // the same rotations go to g now and to the first k + 1 rows of every later column
+        std::vector<cd> Hw = Hn[i];
+        for (int col = 0; col < kc; ++col)
+          for (int row = kc; row > col; --row) {
+            cd cc, ss;
+            const cd rv = givens(Hw[(size_t)col * (kc + 1) + row - 1], Hw[(size_t)col * (kc + 1) + row], cc, ss);
+            for (int c2 = col; c2 < kc; ++c2) rot(Hw, row - 1, cc, ss, (size_t)c2 * (kc + 1));
+            Hw[(size_t)col * (kc + 1) + row - 1] = rv;
+            Hw[(size_t)col * (kc + 1) + row] = 0.0;
+            rot(gv[i], row - 1, cc, ss, 0);
+            qrow[i].push_back(row - 1);
+            qc[i].push_back(cc);
+            qs[i].push_back(ss);
+          }
+        for (int col = 0; col < kc; ++col)
+          for (int row = 0; row <= kc; ++row) R[i][(size_t)col * ldh + row] = Hw[(size_t)col * (kc + 1) + row];
+      }
+    }
     int j;
-    for (j = 0; j < m && total < maxit; ++j) {
+    for (j = kc; j < mk && j - kc < m && total < maxit; ++j) {
       if (prec) precond_apply(c, V.v[j], Z.v[j]);
       apply_A(Z.v[j], w);
       std::vector<cd> h((j + 1) * n, 0.0);
@@ -418,12 +587,11 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
       // count on the propagator and the 16^3x32 workloads (the FP64 outer residual checks anyway).
       {
         multi_cdot(g, V, j + 1, w, kred, s);
-        GBC_CUDA(cudaMemcpyAsync(c->h_kresult, c->d_kresult, sizeof(double) * 2 * (j + 1) * n, cudaMemcpyDeviceToHost, s));
-        sync(c);
+        std::vector<cd> dots = fetch_dots(j + 1);
         std::vector<cd> hp((j + 1) * n);
         for (int q = 0; q <= j; ++q)
           for (int i = 0; i < n; ++i) {
-            cd v(c->h_kresult[(q * 2 + 0) * n + i], c->h_kresult[(q * 2 + 1) * n + i]);
+            cd v = dots[q * n + i];
             if (cyc_done[i]) v = 0.0;
             hp[q * n + i] = -v;
             h[q * n + i] += v;
@@ -434,41 +602,21 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
       std::vector<double> wn2 = norm2(c, w);
       ++total;
       std::vector<cd> inv(n, 0.0);
-      bool all_c = true;
       for (int i = 0; i < n; ++i) {
         if (cyc_done[i]) continue;
         ++st.iters[i];
         const double wn = std::sqrt(wn2[i]);
         std::vector<cd>& Ri = R[i];
-        for (int q = 0; q <= j; ++q) Ri[j * (m + 1) + q] = h[q * n + i];
-        Ri[j * (m + 1) + j + 1] = wn;
-        // previous rotations on the new column
-        for (int q = 0; q < j; ++q) {
-          cd A = Ri[j * (m + 1) + q], B = Ri[j * (m + 1) + q + 1];
-          Ri[j * (m + 1) + q] = std::conj(gc[i][q]) * A + std::conj(gs[i][q]) * B;
-          Ri[j * (m + 1) + q + 1] = -gs[i][q] * A + gc[i][q] * B;
-        }
-        // new rotation (Givens, syssolver_linop_fgmres_dr.h:31-148)
-        cd f = Ri[j * (m + 1) + j], gg = Ri[j * (m + 1) + j + 1], rv;
-        if (f == 0.0) {
-          gc[i][j] = 0.0;
-          gs[i][j] = 1.0;
-          rv = gg;
-        } else if (gg == 0.0) {
-          gs[i][j] = 0.0;
-          gc[i][j] = std::conj(f) / std::abs(f);
-          rv = std::abs(f);
-        } else {
-          double t = std::sqrt(std::norm(f) + std::norm(gg));
-          rv = t;
-          gc[i][j] = f / t;
-          gs[i][j] = gg / t;
-        }
-        Ri[j * (m + 1) + j] = rv;
-        Ri[j * (m + 1) + j + 1] = 0.0;
-        cd A = gv[i][j], B = gv[i][j + 1];
-        gv[i][j] = std::conj(gc[i][j]) * A + std::conj(gs[i][j]) * B;
-        gv[i][j + 1] = -gs[i][j] * A + gc[i][j] * B;
+        const size_t col = (size_t)j * ldh;
+        for (int q = 0; q <= j; ++q) H[i][col + q] = Ri[col + q] = h[q * n + i];
+        H[i][col + j + 1] = Ri[col + j + 1] = wn;
+        // the deflated restart's rotations (rows 0 .. k), then the cycle's own
+        for (size_t t = 0; t < qrow[i].size(); ++t) rot(Ri, qrow[i][t], qc[i][t], qs[i][t], col);
+        for (int q = kc; q < j; ++q) rot(Ri, q, gc[i][q], gs[i][q], col);
+        const cd rv = givens(Ri[col + j], Ri[col + j + 1], gc[i][j], gs[i][j]);
+        Ri[col + j] = rv;
+        Ri[col + j + 1] = 0.0;
+        rot(gv[i], j, gc[i][j], gs[i][j], 0);
         dim[i] = j + 1;
         const double est = std::abs(gv[i][j + 1]);
         if (!std::isfinite(est)) {
@@ -479,12 +627,9 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
         // converged, or exact (happy) breakdown of the Arnoldi process
         if (est <= tol * std::sqrt(bb[i]) || wn < 1e-14 * std::sqrt(bb[i])) cyc_done[i] = 1;
         else inv[i] = 1.0 / wn;
-        all_c &= cyc_done[i] != 0;
       }
-      if (j + 1 <= m) {
-        put_coef(inv, 1);
-        blas_cax(g, c->d_kcoef, w, V.v[j + 1], s);
-      }
+      put_coef(inv, 1);
+      blas_cax(g, c->d_kcoef, w, V.v[j + 1], s);
       bool everyone = true;
       for (int i = 0; i < n; ++i) everyone &= cyc_done[i] != 0;
       if (everyone) {
@@ -493,23 +638,26 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
       }
     }
     // least squares R eta = g per right-hand side, then x += Z eta
-    const int jmax = std::min(j, m);
+    const int jmax = std::min(j, mk);
     std::vector<cd> eta((size_t)jmax * n, 0.0);
     for (int i = 0; i < n; ++i) {
       const int d = dim[i];
+      prev_dim[i] = d;
       if (d == 0 || done[i]) continue;
       std::vector<cd> e(d);
       for (int row = d - 1; row >= 0; --row) {
         cd v = gv[i][row];
-        for (int col = row + 1; col < d; ++col) v -= R[i][col * (m + 1) + row] * e[col];
-        e[row] = v / R[i][row * (m + 1) + row];
+        for (int col = row + 1; col < d; ++col) v -= R[i][(size_t)col * ldh + row] * e[col];
+        e[row] = v / R[i][(size_t)row * ldh + row];
       }
       for (int q = 0; q < d; ++q) eta[q * n + i] = e[q];
+      eta_prev[i] = e;
     }
     if (jmax > 0) {
       put_coef(eta, jmax);
       multi_caxpy(g, Z, jmax, c->d_kcoef, x, 1.0, s);
     }
+    ++cycle;
   }
   for (int i = 0; i < n; ++i)
     if (!done[i] && st.status[i] == GBC_OK) st.status[i] = GBC_ERR_NOT_CONVERGED;
@@ -517,6 +665,76 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
 }
 
 }  // namespace
+
+std::vector<int> refine_shifted(gbc_ctx* c, int sloppy, const Spinor& chi, const double* d_shift,
+                                const Spinor& psi, const std::vector<double>& rsd, int max_iter,
+                                std::vector<double>& rr, std::vector<int>& status) {
+  const int D = PREC_DOUBLE, S = PREC_SINGLE;
+  const int n = psi.nrhs;
+  const Geom& g = c->g;
+  cudaStream_t s = c->stream;
+  Spinor r = sub(workspace(c, 760, D, n), 0, n);
+  Spinor t1 = sub(workspace(c, 761, D, n), 0, n);
+  Spinor te = sub(workspace(c, 762, D, n), 0, n);
+  Spinor rs = sub(workspace(c, 763, S, n), 0, n);
+  Spinor es = sub(workspace(c, 764, S, n), 0, n);
+  Spinor chib = chi;  // every right-hand-side index reads the one source
+  chib.nrhs = n;
+  chib.rhs_bytes = 0;
+  chib.norm_rhs_stride = 0;
+  const double chi2 = norm2(c, chi)[0];
+  std::vector<int> iters(n, 0), done(n, 0);
+  status.assign(n, GBC_OK);
+  rr.assign(n, 0.0);
+  std::vector<double> prev(n, HUGE_VAL);
+  for (int outer = 0; outer < 30; ++outer) {
+    // FP64 residual of every shifted system
+    apply_sys(c, D, true, psi, r, t1, te);
+    blas_shift_axpy(g, d_shift, psi, r, s);
+    blas_xmy_norm2(g, chib, r, red(c), s);
+    rr = fetch(c, 1, n);
+    std::vector<int> active(n, 0);
+    bool any = false;
+    double worst = 0.0;
+    int budget = max_iter;
+    for (int q = 0; q < n; ++q) {
+      if (done[q]) continue;
+      if (!std::isfinite(rr[q])) {
+        status[q] = GBC_ERR_NONFINITE;
+        done[q] = 1;
+        continue;
+      }
+      // converged, or a correction that no longer halves the residual (the sloppy floor)
+      if (rr[q] <= rsd[q] * rsd[q] * chi2 || rr[q] > 0.25 * prev[q]) {
+        done[q] = 1;
+        continue;
+      }
+      prev[q] = rr[q];
+      active[q] = 1;
+      any = true;
+      worst = std::max(worst, std::sqrt(rr[q] / chi2) / rsd[q]);
+      budget = std::min(budget, max_iter - iters[q]);
+    }
+    if (!any || budget <= 0) break;
+    // the correction only needs the part of the reduction still missing (with a factor 2 margin)
+    const double itol = std::min(0.1, std::max(1e-6, 0.5 / worst));
+    blas_copy(g, rs, r, s);
+    CgCfg cfg{S, sloppy, itol, budget, 0.1, 1, d_shift};
+    CgStats st = cg_normal(c, cfg, es, rs, true, active);
+    for (int q = 0; q < n; ++q) {
+      if (!active[q]) continue;
+      iters[q] += st.iters[q];
+      if (st.status[q] == GBC_ERR_NONFINITE) {
+        status[q] = GBC_ERR_NONFINITE;
+        done[q] = 1;
+      }
+    }
+    blas_xpy(g, psi, es, s);
+  }
+  for (int q = 0; q < n; ++q)
+    if (status[q] == GBC_OK && !(rr[q] <= rsd[q] * rsd[q] * chi2)) status[q] = GBC_ERR_NOT_CONVERGED;
+  return iters;
+}
 
 int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_canon, const double* chi_canon,
                  gbc_result* res, const std::function<void()>* after_export) {
@@ -528,6 +746,10 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   if (!(p.inner_tol > 0)) p.inner_tol = 1e-6;
   if (p.inner_max_iter <= 0) p.inner_max_iter = p.max_iter;
   if (p.nkrylov <= 0) p.nkrylov = 16;
+  if (p.ndefl < 0 || p.ndefl + std::min(p.nkrylov, kMaxKrylov - 1) > kMaxKrylov - 1) {
+    c->err = "NDefl + NKrylov above 32";
+    return GBC_ERR_ARGS;
+  }
   int sloppy = p.sloppy_precision ? p.sloppy_precision : c->opts.sloppy_precision;
   if (sloppy != PREC_HALF && sloppy != PREC_SINGLE && sloppy != PREC_DOUBLE) return GBC_ERR_ARGS;
   if (p.system < GBC_SYS_MEO || p.system > GBC_SYS_SYM_MDAGM) return GBC_ERR_ARGS;
@@ -535,10 +757,6 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   // the symmetric operator M_s: every solver below runs unchanged, apply_meo applies M_s
   const bool symmetric = p.system == GBC_SYS_SYM || p.system == GBC_SYS_SYM_MDAGM;
   if (symmetric) {
-    if (c->act.twisted) {
-      c->err = "the symmetric operator is not built with a twisted-mass term";
-      return GBC_ERR_ARGS;
-    }
     if (p.use_precond) {
       c->err = "the learned preconditioner approximates M~^-1, not the symmetric operator's inverse";
       return GBC_ERR_ARGS;
@@ -772,7 +990,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
       if (p.solver == GBC_SOLVER_FGMRES && !mdagm) {
         // flexible GMRES on M~ e = r directly (preconditioned by the learned network if loaded)
         blas_zero(g, es, s);
-        st = fgmres(c, pa, sloppy, es, rsl, itol, p.inner_max_iter, p.nkrylov, p.use_precond != 0, active);
+        st = fgmres(c, pa, sloppy, es, rsl, itol, p.inner_max_iter, p.nkrylov, p.ndefl, p.use_precond != 0, active);
       } else if (p.solver == GBC_SOLVER_BICGSTAB && !mdagm && !bicg_fallback) {
         // BiCGStab on M~ e = r directly (no normal equations)
         InnerStats bs = bicgstab(c, pa, sloppy, itol, p.inner_max_iter, p.delta, es, rsl, active);

@@ -50,7 +50,11 @@ using namespace gbc;
 extern "C" int gbc_time_operator(gbc_ctx* c, int op, int prec, int nrhs, int iters, int flush_l2, double* seconds,
                                  double* bytes) {
   if (!c || !seconds || iters < 1 || nrhs < 1 || nrhs > c->max_rhs) return GBC_ERR_ARGS;
-  if (op != GBC_OP_DSLASH && op != GBC_OP_MEO) return GBC_ERR_ARGS;
+  if (op != GBC_OP_DSLASH && op != GBC_OP_MEO && op != GBC_TIME_PRECOND) return GBC_ERR_ARGS;
+  if (op == GBC_TIME_PRECOND && !c->precond) {
+    c->err = "no learned preconditioner loaded";
+    return GBC_ERR_PRECOND;
+  }
   if (prec != GBC_PREC_DOUBLE && prec != GBC_PREC_SINGLE && prec != GBC_PREC_HALF) return GBC_ERR_ARGS;
   if (!c->have_gauge) {
     c->err = "load the gauge field first";
@@ -72,7 +76,8 @@ extern "C" int gbc_time_operator(gbc_ctx* c, int op, int prec, int nrhs, int ite
     double total = 0.0;
     auto launch = [&]() {
       if (op == GBC_OP_DSLASH) hop(c, prec, 1, HOP_PLAIN, false, 1.0, in, out, nullptr, nullptr, false);
-      else apply_meo(c, prec, false, in, out, te, false);
+      else if (op == GBC_OP_MEO) apply_meo(c, prec, false, in, out, te, false);
+      else precond_apply(c, in, out);
     };
     launch();  // warm-up (module load, first-touch)
     for (int i = 0; i < iters; ++i) {
@@ -94,7 +99,17 @@ extern "C" int gbc_time_operator(gbc_ctx* c, int op, int prec, int nrhs, int ite
       const PrecFields& f = c->pf[pidx(prec)];
       double L = link_bytes(prec, f.recon), S = spinor_bytes(prec), Cb = clover_site_bytes(prec);
       double Vh = c->g.Vh;
-      *bytes = op == GBC_OP_DSLASH ? Vh * (8 * L + 2.0 * nrhs * S) : Vh * (16 * L + 2 * Cb + 5.0 * nrhs * S);
+      if (op == GBC_TIME_PRECOND) {
+        // per layer: the FP32 links of every site once, the FP32 activations in and out of every
+        // right-hand side on both parities; plus the odd-site input and output spinors
+        const double V = (double)c->V;
+        double b = 2.0 * nrhs * Vh * S;
+        for (int l = 0; l < precond_layers(c); ++l)
+          b += V * 288.0 + nrhs * V * 24.0 * (precond_channels(c, l, false) + precond_channels(c, l, true));
+        *bytes = b;
+      } else {
+        *bytes = op == GBC_OP_DSLASH ? Vh * (8 * L + 2.0 * nrhs * S) : Vh * (16 * L + 2 * Cb + 5.0 * nrhs * S);
+      }
     }
     return GBC_OK;
   } catch (const CudaError& e) {

@@ -20,6 +20,7 @@ ERRORS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "solver did not co
 PREC_HALF, PREC_SINGLE, PREC_DOUBLE = 2, 4, 8
 RECON_18, RECON_12 = 18, 12
 OP_DSLASH, OP_CLOVER, OP_CLOVINV, OP_MEO, OP_MDAGM, OP_UNPREC, OP_SYM, OP_SYM_MDAGM = range(8)
+TIME_PRECOND = 100  # gbc_time_operator: one application of the learned preconditioner
 SOLVER_CG, SOLVER_RELIABLE_CG, SOLVER_MIXED, SOLVER_FGMRES, SOLVER_BICGSTAB = range(5)
 SYS_MEO, SYS_MDAGM, SYS_FULL, SYS_SYM, SYS_SYM_MDAGM = range(5)
 BLAS_NORM2, BLAS_CDOT, BLAS_CG_UPDATE, BLAS_XPAY, BLAS_BICG_XR = range(5)
@@ -56,7 +57,7 @@ class SolveParams(C.Structure):
     _fields_ = [("solver", C.c_int), ("system", C.c_int), ("rsd_target", C.c_double), ("max_iter", C.c_int),
                 ("delta", C.c_double), ("rsd_tolerance_factor", C.c_double), ("sloppy_precision", C.c_int),
                 ("inner_tol", C.c_double), ("inner_max_iter", C.c_int), ("nkrylov", C.c_int),
-                ("use_precond", C.c_int), ("zero_guess", C.c_int)]
+                ("use_precond", C.c_int), ("zero_guess", C.c_int), ("ndefl", C.c_int)]
 
 
 class Result(C.Structure):
@@ -239,13 +240,13 @@ class Context:
 
     def solve(self, chi, solver=SOLVER_CG, system=SYS_MEO, rsd_target=1e-10, max_iter=10000, delta=0.1,
               sloppy_precision=0, inner_tol=0.0, nkrylov=16, use_precond=0, psi0=None, tol_factor=10.0,
-              raise_on_error=True):
+              raise_on_error=True, ndefl=0):
         chi = self._fields(chi)
         nrhs = chi.shape[0]
         psi = np.zeros_like(chi) if psi0 is None else self._fields(psi0).copy()
         p = SolveParams(int(solver), int(system), float(rsd_target), int(max_iter), float(delta), float(tol_factor),
                         int(sloppy_precision), float(inner_tol), 0, int(nkrylov), int(use_precond),
-                        int(psi0 is None))
+                        int(psi0 is None), int(ndefl))
         res = (Result * nrhs)()
         rc = self.lib.gbc_solve(self.h, C.byref(p), nrhs, _dp(psi.view(np.float64)), _dp(chi.view(np.float64)), res)
         if rc != GBC_OK and raise_on_error:
@@ -253,16 +254,17 @@ class Context:
         return psi, [r.as_dict() for r in res], rc
 
     def solve_multishift(self, chi, shifts, rsd_target=1e-10, rsd_targets=None, max_iter=10000, tol_factor=10.0,
-                         raise_on_error=True):
-        """(M~^dag M~ + shift_s) psi_s = chi for every shift (odd sites); returns psi (ns, V, 12)."""
+                         raise_on_error=True, sloppy_precision=0):
+        """(M~^dag M~ + shift_s) psi_s = chi for every shift (odd sites); returns psi (ns, V, 12).
+        sloppy_precision PREC_HALF / PREC_SINGLE: FP32 recursion plus per-shift FP64 refinement."""
         chi = np.ascontiguousarray(chi, dtype=np.complex128).reshape(self.V, 12)
         ns = len(shifts)
         psi = np.zeros((ns, self.V, 12), dtype=np.complex128)
         sh = (C.c_double * ns)(*[float(x) for x in shifts])
         rt = None if rsd_targets is None else (C.c_double * ns)(*[float(x) for x in rsd_targets])
         pp = (C.POINTER(C.c_double) * ns)(*[_dp(psi[k].view(np.float64)) for k in range(ns)])
-        p = SolveParams(SOLVER_CG, SYS_MDAGM, float(rsd_target), int(max_iter), 0.1, float(tol_factor), 0, 0.0, 0,
-                        16, 0, 1)
+        p = SolveParams(SOLVER_CG, SYS_MDAGM, float(rsd_target), int(max_iter), 0.1, float(tol_factor),
+                        int(sloppy_precision), 0.0, 0, 16, 0, 1)
         res = (Result * ns)()
         rc = self.lib.gbc_solve_multishift(self.h, C.byref(p), ns, sh, rt, pp, _dp(chi.view(np.float64)), res)
         if rc != GBC_OK and raise_on_error:
@@ -271,10 +273,10 @@ class Context:
 
     def solve_device(self, psi_ptr, chi_ptr, nrhs, solver=SOLVER_CG, system=SYS_MEO, rsd_target=1e-10,
                      max_iter=10000, delta=0.1, sloppy_precision=0, inner_tol=0.0, nkrylov=16, use_precond=0,
-                     zero_guess=True, tol_factor=10.0):
+                     zero_guess=True, tol_factor=10.0, ndefl=0):
         p = SolveParams(int(solver), int(system), float(rsd_target), int(max_iter), float(delta), float(tol_factor),
                         int(sloppy_precision), float(inner_tol), 0, int(nkrylov), int(use_precond),
-                        int(bool(zero_guess)))
+                        int(bool(zero_guess)), int(ndefl))
         res = (Result * nrhs)()
         rc = self.lib.gbc_solve_device(self.h, C.byref(p), int(nrhs), C.c_void_p(psi_ptr), C.c_void_p(chi_ptr), res)
         return [r.as_dict() for r in res], rc

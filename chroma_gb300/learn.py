@@ -8,6 +8,7 @@ low modes the Krylov method resolves last) form the training pairs, x* the FP64 
 configurations, and saved in the versioned weights format of gbc_precond_save.
 
     python -m chroma_gb300.learn --dims 16,16,16,32 --kappa 0.115 --csw 1.0 --out weights.gbcw
+    python -m chroma_gb300.learn --config5 weights/cnn_32x32x32x64 --configs 2 --samples 8 --rounds 3
 """
 import argparse
 import json
@@ -85,6 +86,50 @@ def ablation(ctx, dims, seed=77, rsd=1e-10, sloppy=G.PREC_SINGLE, kappa=None):
     return out
 
 
+def network_seconds(ctx, nrhs, prec=G.PREC_SINGLE, iters=5):
+    """Device time of one application of the loaded network to nrhs odd-site fields (CUDA events)."""
+    sec, _ = ctx.time_operator(G.TIME_PRECOND, prec, nrhs=nrhs, iters=iters, flush_l2=True)
+    return sec
+
+
+def propagator_study(ctx, dims, seed=999_999, eps=0.3, rsd=1e-10, sloppy=G.PREC_HALF, nkrylov=16):
+    """The 12 point sources of one held-out configuration solved as one batch of the full system
+    (FP64 defect correction, mixed precision): FGMRES(nkrylov) with and without the loaded
+    network, and the reliable BiCGStab without it, on the same context."""
+    ctx.load_gauge(G.gauge_synthetic(dims, eps, seed, t_boundary=-1))
+    src = S.point_sources(dims).reshape(12, -1, 12)
+    out = {}
+    runs = (("fgmres_with_net", dict(solver=G.SOLVER_FGMRES, use_precond=1, nkrylov=nkrylov)),
+            ("fgmres_without_net", dict(solver=G.SOLVER_FGMRES, use_precond=0, nkrylov=nkrylov)),
+            ("bicgstab_without_net", dict(solver=G.SOLVER_BICGSTAB, delta=0.01, inner_tol=1e-5)))
+    for name, kw in runs:
+        _, res, rc = ctx.solve(src, system=G.SYS_FULL, rsd_target=rsd, sloppy_precision=sloppy, raise_on_error=False,
+                               **kw)
+        out[name] = {"inner_iterations_max": max(r["n_count"] for r in res), "device_seconds": res[0]["device_seconds"],
+                     "true_rel_resid_max": max(r["rel_resid"] for r in res), "status": rc}
+    out["network_seconds_12rhs"] = network_seconds(ctx, 12)
+    return out
+
+
+def config5(out_prefix, configs=2, samples=8, full_pairs=8, rounds=3, epochs=4, log=print):
+    """The learned preconditioner at the 32^3 x 64 propagator workload (kappa 0.125, c_sw 1.6):
+    trained on this volume with the low-mode pairs of 50 CG iterations alone, and with as many
+    full-inverse pairs added; each network studied on a held-out configuration's 12-source solve."""
+    dims, kappa, csw = (32, 32, 32, 64), 0.125, 1.6
+    result = {}
+    for variant, fp in (("low_mode", 0), ("low_mode_and_full_inverse", full_pairs)):
+        t0 = time.time()
+        ctx, hist = train(dims, kappa, csw, configs=configs, samples=samples, cg_iters=50, rounds=rounds,
+                          epochs=epochs, out=f"{out_prefix}_{variant}.gbcw", log=log, full_pairs=fp)
+        train_s = time.time() - t0
+        study = propagator_study(ctx, dims)
+        result[variant] = {"training_seconds": train_s, "loss_history": hist, "pairs_per_config": samples + fp,
+                           "configs": configs, **study}
+        log(json.dumps({variant: result[variant]}))
+        ctx.close()
+    return result
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--dims", default="16,16,16,32")
@@ -98,7 +143,13 @@ def main():
     ap.add_argument("--cg-iters", type=int, default=50)
     ap.add_argument("--full-pairs", type=int, default=0)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--config5", default=None, metavar="PREFIX",
+                    help="train and study the network at 32^3x64 (kappa 0.125, c_sw 1.6); weights to PREFIX_*.gbcw")
     a = ap.parse_args()
+    if a.config5:
+        print(json.dumps(config5(a.config5, configs=a.configs, samples=a.samples, full_pairs=a.full_pairs or a.samples,
+                                 rounds=a.rounds, epochs=a.epochs)))
+        return
     dims = tuple(int(x) for x in a.dims.split(","))
     ctx, hist = train(dims, a.kappa, a.csw, configs=a.configs, samples=a.samples, rounds=a.rounds, epochs=a.epochs,
                       lr=a.lr, out=a.out, cg_iters=a.cg_iters, full_pairs=a.full_pairs)

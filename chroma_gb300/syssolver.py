@@ -4,7 +4,7 @@ Mirrors, for Python callers and for the tests, the interface that the C++ adapte
 ``chroma_plugin/`` gives Chroma:
 
 - ``SysSolverGB300CloverParams``: the QUDA clover XML schema (syssolver_quda_clover_params.cc:12-131)
-  plus optional tags (SolverType MIXED/FGMRES/BICGSTAB, NKrylov, PrecondWeights, InnerTol);
+  plus optional tags (SolverType MIXED/FGMRES/BICGSTAB, NKrylov, NDefl, PrecondWeights, InnerTol);
   QUDA's GCR maps to FGMRES (both minimise the residual over a flexible Krylov space);
 - ``TheLinOpFermSystemSolverFactory`` / ``TheMdagMFermSystemSolverFactory``: string-keyed
   factories (syssolver_linop_factory.h:29-39, syssolver_mdagm_factory.h:28-39) with the entry
@@ -114,6 +114,7 @@ class SysSolverGB300CloverParams:
     BackupSolverParam: str = None
     Verbose: bool = False
     NKrylov: int = 16
+    NDefl: int = 0
     PrecondWeights: str = None
     InnerTol: float = 1e-6
 
@@ -139,6 +140,7 @@ class SysSolverGB300CloverParams:
         p.BackupSolverParam = ET.tostring(bk, encoding="unicode") if bk is not None else None
         p.Verbose = node.findtext("Verbose", "false").strip().lower() == "true"
         p.NKrylov = int(node.findtext("NKrylov", "16"))
+        p.NDefl = int(node.findtext("NDefl", "0"))
         p.PrecondWeights = node.findtext("PrecondWeights")
         p.InnerTol = float(node.findtext("InnerTol", "1e-6"))
         return p
@@ -181,7 +183,8 @@ class _Base:
         out, res, rc = self.ctx.solve(chi, solver=_SOLVER[p.SolverType], system=self.system, rsd_target=p.RsdTarget,
                                       max_iter=p.MaxIter, delta=p.Delta,
                                       sloppy_precision=_PREC[p.CudaSloppyPrecision], inner_tol=p.InnerTol,
-                                      nkrylov=p.NKrylov, use_precond=int(bool(p.PrecondWeights)), psi0=psi,
+                                      nkrylov=p.NKrylov, ndefl=p.NDefl, use_precond=int(bool(p.PrecondWeights)),
+                                      psi0=psi,
                                       tol_factor=p.RsdToleranceFactor, raise_on_error=False)
         results = [SystemSolverResults_t(r["n_count"], r["resid"], r["rel_resid"], r["status"], r["seconds"])
                    for r in res]

@@ -66,6 +66,7 @@ namespace Chroma
     q.inner_tol = toDouble(p.InnerTol);
     q.inner_max_iter = 0;
     q.nkrylov = p.NKrylov;
+    q.ndefl = p.NDefl;
     q.use_precond = p.PrecondWeights.empty() ? 0 : 1;
     q.zero_guess = 1;  // quarkProp4_a starts every source from psi = zero
     std::vector<gbc_result> res(n);

@@ -8,7 +8,7 @@ namespace Chroma
   SysSolverGB300CloverParams::SysSolverGB300CloverParams()
     : MaxIter(10000), RsdTarget(1.0e-10), AntiPeriodicT(true), Delta(0.1), SolverType("MIXED"),
       CudaSloppyPrecision("HALF"), CudaSloppyReconstruct("RECONS_12"), RsdToleranceFactor(10),
-      SilentFail(false), backup_invP(false), verboseP(false), NKrylov(16), InnerTol(1.0e-6), MaxRHS(12)
+      SilentFail(false), backup_invP(false), verboseP(false), NKrylov(16), NDefl(0), InnerTol(1.0e-6), MaxRHS(12)
   {}
 
   SysSolverGB300CloverParams::SysSolverGB300CloverParams(XMLReader& xml, const std::string& path)
@@ -32,6 +32,7 @@ namespace Chroma
     }
     if (paramtop.count("Verbose") > 0) read(paramtop, "Verbose", verboseP);
     if (paramtop.count("NKrylov") > 0) read(paramtop, "NKrylov", NKrylov);
+    if (paramtop.count("NDefl") > 0) read(paramtop, "NDefl", NDefl);
     if (paramtop.count("InnerTol") > 0) read(paramtop, "InnerTol", InnerTol);
     if (paramtop.count("PrecondWeights") > 0) read(paramtop, "PrecondWeights", PrecondWeights);
     if (paramtop.count("MaxRHS") > 0) read(paramtop, "MaxRHS", MaxRHS);
@@ -61,6 +62,7 @@ namespace Chroma
     write(xml, "RsdToleranceFactor", p.RsdToleranceFactor);
     write(xml, "SilentFail", p.SilentFail);
     write(xml, "NKrylov", p.NKrylov);
+    write(xml, "NDefl", p.NDefl);
     write(xml, "InnerTol", p.InnerTol);
     if (!p.PrecondWeights.empty()) write(xml, "PrecondWeights", p.PrecondWeights);
     pop(xml);

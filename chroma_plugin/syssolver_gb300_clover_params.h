@@ -5,7 +5,8 @@
  *  The XML layout is the one of SysSolverQUDACloverParams
  *  (lib/actions/ferm/invert/quda_solvers/syssolver_quda_clover_params.{h:15-90,cc:12-131}), so an
  *  existing QUDA_CLOVER_INVERTER input runs after changing <invType> only.  Optional tags:
- *  SolverType MIXED | BICGSTAB | FGMRES | GCR | RELIABLE_CG | CG, NKrylov, InnerTol, PrecondWeights, MaxRHS.
+ *  SolverType MIXED | BICGSTAB | FGMRES | GCR | RELIABLE_CG | CG, NKrylov, NDefl, InnerTol, PrecondWeights,
+ *  MaxRHS.
  *  Compiled only inside a Chroma build (needs QDP++).
  */
 #ifndef __syssolver_gb300_clover_params_h__
@@ -38,6 +39,7 @@ namespace Chroma
     GroupXML_t backup_inv_param;
     bool verboseP;
     int NKrylov;
+    int NDefl;  //!< FGMRES-DR deflation space (FGMRESDR_INVERTER's NDefl)
     Real InnerTol;
     std::string PrecondWeights;       // empty: no learned preconditioner
     int MaxRHS;

@@ -62,8 +62,9 @@ extern "C" {
 #define GBC_SOLVER_MIXED 2        /* RICHARDSON_MP_CLOVER_INVERTER pattern: FP64 defect correction
                                      around a reliable-update CGNE in sloppy precision
                                      (inv_multiprec_richardson.cc:13-107)                            */
-#define GBC_SOLVER_FGMRES 3       /* FGMRESDR_INVERTER with NDefl = 0 (syssolver_linop_fgmres_dr.cc),
-                                     preconditioned by the learned network when loaded               */
+#define GBC_SOLVER_FGMRES 3       /* FGMRESDR_INVERTER (syssolver_linop_fgmres_dr.cc): NKrylov, NDefl
+                                     (deflated restarts), preconditioned by the learned network when
+                                     loaded                                                          */
 #define GBC_SOLVER_BICGSTAB 4     /* FP64 defect correction around a reliable BiCGStab on M~ in the
                                      sloppy precision: RELIABLE_BICGSTAB_MP_CLOVER_INVERTER
                                      (reliable_bicgstab.cc:93-277), QUDA SolverType BICGSTAB.  The
@@ -75,7 +76,8 @@ extern "C" {
 #define GBC_SYS_FULL 2   /* M psi = chi on both parities: Schur prep, odd solve, even reconstruction
                             (PrecFermActQprop, eoprec_fermact_qprop.cc:41-80)                        */
 #define GBC_SYS_SYM 3    /* M_s psi_o = chi_o for the symmetric operator SEOPREC_CLOVER
-                            (SymEvenOddPrecCloverLinOp, seoprec_clover_linop_w.cc:145-187); no twist */
+                            (SymEvenOddPrecCloverLinOp, seoprec_clover_linop_w.cc:145-187), with
+                            + isign i mu gamma_5 when twisted (:174-184)                            */
 #define GBC_SYS_SYM_MDAGM 4 /* M_s^dag M_s psi_o = chi_o (MdagM solver of a SEOPREC action)            */
 
 /* ---- parameter structs ------------------------------------------------------------------- */
@@ -119,6 +121,9 @@ typedef struct gbc_solve_params {
   int nkrylov;                /* FGMRES NKrylov (0 = 16)                            */
   int use_precond;            /* FGMRES: apply the loaded learned preconditioner     */
   int zero_guess;             /* 1: ignore psi on entry (qprop passes zero)          */
+  int ndefl;                  /* FGMRES NDefl: harmonic Ritz vectors carried across
+                                 restarts (FGMRES-DR); 0 = plain restarts; at most
+                                 32 - NKrylov                                      */
 } gbc_solve_params;
 
 /* SystemSolverResults_t (lib/syssolver.h:16-23) plus what the adapter logs */
@@ -228,6 +233,10 @@ const char* gbc_batch_last_error(gbc_batch* batch);
    with L, S, C the stored bytes of a link, a spinor (+ its norm in half) and a clover site. */
 int gbc_time_operator(gbc_ctx* ctx, int op, int prec, int nrhs, int iters, int flush_l2, double* seconds,
                       double* bytes);
+/* op code of gbc_time_operator for one application of the loaded learned preconditioner to nrhs
+   odd-site fields (no Chroma counterpart); bytes = per layer the FP32 links of every site once and
+   the FP32 activations in and out of every right-hand side, plus the input and output spinors */
+#define GBC_TIME_PRECOND 100
 
 /* ---- no-allocation operator ----------------------------------------------------------------- */
 /* No counterpart in the reference.  The even-odd operator M~ (as gbc_apply with GBC_OP_MEO and
@@ -291,8 +300,13 @@ int gbc_gauge_synthetic(const int dims[4], double eps, unsigned long long seed, 
    replaces MdagMMultiSysSolverCG::operator()(psi, shifts, chi)
    (lib/actions/ferm/invert/multi_syssolver_mdagm_cg.h:58-80) and its MInvCG2
    (lib/actions/ferm/invert/minvcg2.cc:70-357), same recursion and stopping rule, FP64.
-   shifts[s] >= 0; rsd_targets[s] is RsdCG per shift (NULL: p->rsd_target for all); p->max_iter
-   and p->rsd_tolerance_factor are used, the other fields of p are ignored.  chi and every psi[s]
+   shifts[s] >= 0; rsd_targets[s] is RsdCG per shift (NULL: p->rsd_target for all); p->max_iter,
+   p->rsd_tolerance_factor and p->sloppy_precision are used, the other fields of p are ignored.
+   sloppy_precision GBC_PREC_HALF or GBC_PREC_SINGLE selects the mixed-precision form (the
+   multiprec pattern of Chroma's multi-shift solvers): the shared-Krylov recursion on FP32 fields to
+   a relative 1e-6, then an FP64 defect correction of every shift, batched over the shifts, with
+   corrections from CG on the shifted system in the sloppy operator (n_count adds those iterations);
+   0 or GBC_PREC_DOUBLE runs the recursion in FP64 to the targets.  chi and every psi[s]
    are canonical host arrays (only their odd sites are read / written); res[s] per shift, with the
    FP64 true relative residual of that shifted system. */
 int gbc_solve_multishift(gbc_ctx* ctx, const gbc_solve_params* p, int nshift, const double* shifts,

@@ -67,3 +67,20 @@ def test_per_shift_targets_and_bad_arguments(setup):
     assert _rel(op, psi[1], chi, 2.0) <= 1.5e-11
     with pytest.raises(G.GBCError):
         ctx.solve_multishift(chi, [-1.0])
+
+
+@pytest.mark.parametrize("sloppy", [G.PREC_SINGLE, G.PREC_HALF], ids=["f32", "f16"])
+def test_mixed_precision_multishift(setup, sloppy):
+    """The mixed-precision form (FP32 recursion, then the FP64 defect correction of every shift with
+    corrections from the shifted CG in the sloppy operator): every shift meets its FP64 target as
+    recomputed by the oracle, and the solutions agree with the FP64 multi-shift ones."""
+    dims, op, ctx = setup
+    chi = S.z2_noise(dims, 14, cb=1).reshape(-1, 12)
+    shifts = [0.0, 0.02, 0.3, 2.0]
+    psi, res, rc = ctx.solve_multishift(chi, shifts, rsd_target=1e-10, sloppy_precision=sloppy)
+    assert rc == 0, res
+    ref, _, _ = ctx.solve_multishift(chi, shifts, rsd_target=1e-12)
+    for k, sigma in enumerate(shifts):
+        assert _rel(op, psi[k], chi, sigma) <= 1.5e-10, (sigma, res[k])
+        assert res[k]["status"] == 0 and res[k]["n_outer"] == 1
+        assert np.linalg.norm(psi[k] - ref[k]) / np.linalg.norm(ref[k]) < 1e-8

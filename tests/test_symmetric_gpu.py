@@ -1,7 +1,8 @@
 """The symmetric even-odd operator M_s = 1 - 1/4 A_oo^-1 D_oe A_ee^-1 D_eo (SEOPREC_CLOVER,
 seoprec_clover_linop_w.cc:145-187) on the GPU against the CPU oracle: operator parity in FP64 / FP32
-/ FP16 (1e-12 / 1e-6 / 5e-3 relative), the odd clover inverse, and solves of M_s psi = chi and of
-M_s^dag M_s psi = chi that reach the oracle's FP64 residual 1e-10."""
+/ FP16 (1e-12 / 1e-6 / 5e-3 relative), the odd clover inverse, solves of M_s psi = chi and of
+M_s^dag M_s psi = chi that reach the oracle's FP64 residual 1e-10, and the same with a twisted-mass
+term."""
 import numpy as np
 import pytest
 
@@ -90,16 +91,39 @@ def test_factory_selects_symmetric_operator(setup):
     solver.ctx.close()
 
 
-def test_symmetric_rejects_twisted_mass():
-    from oracle import Oracle
-    dims = (4, 4, 4, 4)
+@pytest.mark.parametrize("prec", [G.PREC_DOUBLE, G.PREC_SINGLE, G.PREC_HALF], ids=["f64", "f32", "f16"])
+def test_symmetric_twisted_operator_and_solves(prec):
+    """M_s + isign i mu gamma_5 (seoprec_clover_linop_w.cc:174-184; the clover term and its inverses
+    carry no twist) against the oracle for both isigns, and solves of M psi = chi and
+    M^dag M psi = chi that reach the oracle's FP64 residual 1e-10."""
+    from oracle import Oracle, OracleOp
+    from oracle import oracle as O
+    dims = (4, 6, 4, 8)
+    mu = 0.05
     o = Oracle()
-    u = o.apply_bc(dims, o.gauge_hot(dims, 0.3, 1), (1, 1, 1, -1))
-    ctx = G.Context(dims, 0.1, 1.0, t_boundary=-1, max_rhs=1, twisted_m=0.05)
+    u = o.apply_bc(dims, o.gauge_hot(dims, 0.3, 809), (1, 1, 1, -1))
+    mass = 1 / (2 * KAPPA) - 4
+    op = OracleOp(dims, u, mass, CSW, twisted_m=mu)
+    ctx = G.Context(dims, mass, CSW, t_boundary=-1, max_rhs=3, twisted_m=mu)
     try:
         ctx.load_gauge(u)
-        chi = S.z2_noise(dims, 2, cb=1).reshape(1, -1, 12)
-        with pytest.raises(G.GBCError):
-            ctx.solve(chi, solver=G.SOLVER_CG, system=G.SYS_SYM)
+        V = int(np.prod(dims))
+        par = S.parity(dims)
+        xs = np.stack([S.gaussian(dims, 90 + k).reshape(V, 12) for k in range(3)])
+        for gop, oop, isign in [(G.OP_SYM, O.OP_SYM, 1), (G.OP_SYM, O.OP_SYM, -1),
+                                (G.OP_SYM_MDAGM, O.OP_SYM_MDAGM, 1)]:
+            got = ctx.apply(gop, xs, isign, 1, prec)
+            for k in range(3):
+                want = op.apply(oop, xs[k], isign, 1)
+                assert rel(got[k][par == 1], want[par == 1]) < TOL[prec], (gop, isign, k)
+        if prec != G.PREC_DOUBLE:
+            return
+        chi = S.z2_noise(dims, 91, cb=1).reshape(1, -1, 12)
+        for solver, sloppy, system, oop in [(G.SOLVER_BICGSTAB, G.PREC_HALF, G.SYS_SYM, O.OP_SYM),
+                                            (G.SOLVER_MIXED, G.PREC_HALF, G.SYS_SYM_MDAGM, O.OP_SYM_MDAGM)]:
+            psi, res, rc = ctx.solve(chi, solver=solver, system=system, rsd_target=1e-10, sloppy_precision=sloppy)
+            assert rc == 0, res
+            r = chi[0] - op.apply(oop, psi[0], +1, 1)
+            assert np.sqrt(op.norm2(r) / op.norm2(chi[0])) <= 1.05e-10
     finally:
         ctx.close()
