@@ -282,6 +282,31 @@ def chroma_factory_path(ctx, G, op, src, solve_kw):
 
 
 WEIGHTS = os.path.join(ROOT, "chroma_gb300", "weights", "cnn_16x16x16x32_k0.115_csw1.0.gbcw")
+# the network retrained on this workload's volume and action (32^3 x 64, kappa 0.125, c_sw 1.6) from
+# low-mode and full-inverse pairs on two configurations other than the benchmark's
+WEIGHTS32 = os.path.join(ROOT, "chroma_gb300", "weights", "cnn_32x32x32x64_k0.125_csw1.6.gbcw")
+
+
+def learned_headline(ctx, G, chi_d, nsrc, plain_s):
+    """The benchmark spec's full form on the headline workload: the learned preconditioner inside
+    FGMRES(16) (flexible, right-preconditioned), mixed precision (FP64 defect correction, FP16
+    operator), the 12 sources as one batch; against plain FP64 CG on the same GPU.  Also one
+    application of the network to the 12 sources and the same FGMRES without it."""
+    import torch
+    if not os.path.exists(WEIGHTS32):
+        return None
+    ctx.load_precond(WEIGHTS32)
+    out = {"weights": os.path.basename(WEIGHTS32)}
+    psi = torch.zeros_like(chi_d)
+    for name, use in (("fgmres_with_net", 1), ("fgmres_without_net", 0)):
+        res, rc = ctx.solve_device(psi.data_ptr(), chi_d.data_ptr(), nsrc, solver=G.SOLVER_FGMRES, system=G.SYS_FULL,
+                                   rsd_target=RSD, sloppy_precision=G.PREC_HALF, nkrylov=16, use_precond=use)
+        out[name] = {"seconds": res[0]["device_seconds"], "inner_iterations_max": max(r["n_count"] for r in res),
+                     "true_rel_resid_max": max(r["rel_resid"] for r in res), "rc": rc}
+    out["speedup_vs_plain_cg"] = plain_s / out["fgmres_with_net"]["seconds"] if plain_s else None
+    sec, _ = ctx.time_operator(G.TIME_PRECOND, G.PREC_SINGLE, nrhs=nsrc, iters=3, flush_l2=True)
+    out["network_application_12rhs_s"] = sec
+    return out
 
 
 def side_workloads(G):
@@ -289,7 +314,8 @@ def side_workloads(G):
     - stout16: 16^3x32, eps 0.2 + 4 stout steps rho 0.1, kappa 0.12, c_sw 1.2, one Gaussian source:
       mixed FP16/FP64 (inner CGNE and inner BiCGStab) vs plain FP64 CG on the same GPU;
     - uneven_batch: 8^3x16, 12^3x24, 16^3x32, 20^3x40 (kappa 0.124, c_sw 1.5, one Z2 source each)
-      solved as one batch (one multi-lattice stencil launch per application) vs one by one;
+      solved as one batch vs one by one; the batch runs its inner iterations as the persistent
+      kernel (batched_*) and as one launch per step replayed from graphs (batched_graphs_*);
     - learned16: 16^3x32, kappa 0.115, c_sw 1.0, FGMRES(16) with and without the trained network on
       a gauge configuration outside its training set."""
     from chroma_gb300 import sources as S
@@ -324,11 +350,16 @@ def side_workloads(G):
         ctxs.append(c)
         chis.append(S.z2_noise(d, 8000 + k, cb=1).reshape(-1, 12))
     batch = G.Batch(ctxs)
-    batch.solve(chis, rsd_target=RSD)
-    tb = []
-    for _ in range(3):
-        _, res = batch.solve(chis, rsd_target=RSD)
-        tb.append(res[0]["device_seconds"])
+    paths = {}
+    for mode in ("0", "1"):  # per-launch (graph-replayed) path, then the persistent kernel
+        os.environ["GBC_PERSISTENT"] = mode
+        batch.solve(chis, rsd_target=RSD)
+        tb = []
+        for _ in range(3):
+            _, res = batch.solve(chis, rsd_target=RSD)
+            tb.append(res[0]["device_seconds"])
+        paths[mode] = (statistics.median(tb), res[0]["launches"])
+    os.environ.pop("GBC_PERSISTENT", None)
     for c, x in zip(ctxs, chis):
         c.solve(x.reshape(1, -1, 12), solver=G.SOLVER_MIXED, rsd_target=RSD)
     ts = []
@@ -339,7 +370,9 @@ def side_workloads(G):
             tot += r1[0]["device_seconds"]
         ts.append(tot)
     out["uneven_batch"] = {"lattices": ["x".join(map(str, d)) for d in lats],
-                           "batched_seconds": statistics.median(tb), "one_by_one_seconds": statistics.median(ts),
+                           "batched_seconds": paths["1"][0], "batched_launches": paths["1"][1],
+                           "batched_graphs_seconds": paths["0"][0], "batched_graphs_launches": paths["0"][1],
+                           "one_by_one_seconds": statistics.median(ts),
                            "true_rel_resid_max": max(r["rel_resid"] for r in res),
                            "iterations": [r["n_count"] for r in res]}
     batch.close()
@@ -491,7 +524,7 @@ def main():
 
     # the same solve with the inner CGNE, and FP64 BiCGStab (12-RHS batch, FP64 defect correction
     # around an FP64 inner BiCGStab): context for the choice of the inner solver
-    inner_cgne, plain_bicg = None, None
+    inner_cgne, plain_bicg, fp64_outer = None, None, None
     if args.plain_steps > 0:
         psi1 = torch.zeros_like(chi_d)
         for _ in range(2):  # the first one tunes the stencil variants that only CGNE uses
@@ -503,6 +536,14 @@ def main():
                                    **dict(solve_kw, sloppy_precision=G.PREC_DOUBLE))
         plain_bicg = {"seconds": res[0]["device_seconds"], "iterations_per_rhs": res[0]["n_count"],
                       "true_rel_resid_max": max(r["rel_resid"] for r in res), "rc": rc}
+        # the same headline solve with its Schur prep and intermediate outer residual in FP64
+        # arithmetic instead of double-float (GBC_OUTER_DF=0)
+        os.environ["GBC_OUTER_DF"] = "0"
+        for _ in range(2):
+            res, rc = ctx.solve_device(psi1.data_ptr(), chi_d.data_ptr(), nsrc, **solve_kw)
+        os.environ.pop("GBC_OUTER_DF", None)
+        fp64_outer = {"seconds": res[0]["device_seconds"], "inner_iterations_per_rhs": res[0]["n_count"],
+                      "true_rel_resid_max": max(r["rel_resid"] for r in res), "rc": rc}
 
     # Roofline of the dominant kernel pair: the FP16 M~ on 12 RHS (the A_ee^-1 D_eo and the
     # A_oo x - 1/4 D_oe t launches the solve runs twice per iteration, 40 % of its time), cold L2
@@ -513,6 +554,9 @@ def main():
     sec1, byts1 = ctx.time_operator(G.OP_DSLASH, G.PREC_HALF, nrhs=1, iters=20, flush_l2=True)
     secm, bytm = ctx.time_operator(G.OP_MEO, G.PREC_HALF, nrhs=1, iters=20, flush_l2=True)
     sec64, byts64 = ctx.time_operator(G.OP_DSLASH, G.PREC_DOUBLE, nrhs=1, iters=10, flush_l2=True)
+    # the outer loop's operator on 12 right-hand sides: FP64 arithmetic and double-float
+    m64, _ = ctx.time_operator(G.OP_MEO, G.PREC_DOUBLE, nrhs=12, iters=3, flush_l2=True)
+    mdf, _ = ctx.time_operator(G.OP_MEO, G.PREC_DF64, nrhs=12, iters=3, flush_l2=True)
     achieved = byts / sec / 1e9
     # DRAM traffic of one such M~: a constant, not measured in this run (ncu cannot run inside the
     # benchmark) -- dram__bytes_read.sum + dram__bytes_write.sum of the M~'s two launches captured
@@ -531,7 +575,8 @@ def main():
             "dslash_12rhs_fp16_gbs": bytd / secd / 1e9, "dslash_12rhs_fp16_frac": bytd / secd / 1e9 / pk["hbm_gbs"],
             "single_rhs_fp16_gbs": byts1 / sec1 / 1e9, "single_rhs_fp16_frac": byts1 / sec1 / 1e9 / pk["hbm_gbs"],
             "single_rhs_meo_fp16_gbs": bytm / secm / 1e9, "single_rhs_meo_fp16_frac": bytm / secm / 1e9 / pk["hbm_gbs"],
-            "single_rhs_fp64_gbs": byts64 / sec64 / 1e9}
+            "single_rhs_fp64_gbs": byts64 / sec64 / 1e9,
+            "meo_12rhs_fp64_s": m64, "meo_12rhs_double_float_s": mdf}
 
     # e2e through the public API with pinned host buffers
     chi_h = torch.from_numpy(src.view(np.float64).copy()).pin_memory()
@@ -569,6 +614,8 @@ def main():
         del op
 
     extras = {} if args.no_extras else side_workloads(G)
+    if not args.no_extras:
+        extras["learned32"] = learned_headline(ctx, G, chi_d, nsrc, plain)
     iters = [r["n_count"] for r in last]
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -581,7 +628,7 @@ def main():
                    "parallelism": f"replicas x{world}"},
         "plain_cg_fp64_s": plain, "speedup_vs_plain_cg": plain / value if (value and plain) else None,
         "iterations": {"mixed_inner_per_rhs_median": int(np.median(iters)), "plain_cg_per_rhs": plain_iters},
-        "same_solve_inner_cgne": inner_cgne,
+        "same_solve_inner_cgne": inner_cgne, "same_solve_fp64_outer_steps": fp64_outer,
         "plain_bicgstab_fp64_batched": plain_bicg,
         "true_rel_resid_max": max(r["rel_resid"] for r in last),
         "plain_cg_true_rel_resid_max": max(plain_res) if plain else None,

@@ -4,9 +4,13 @@
 // defect correction runs per lattice; the inner reliable-update CGNE runs for all lattices in
 // lock step, and each of its stencil applications is ONE launch over a work table of
 // (lattice, 128-site block) pairs covering all lattices (hop_kernel_multi), so small lattices do
-// not leave the GPU idle.  The iteration blocks are replayed from a CUDA graph.
+// not leave the GPU idle.  By default the inner iterations run as a persistent cooperative kernel
+// (batch_persistent.cuh) that performs up to 256 iterations per launch and returns only for a
+// reliable update or convergence; GBC_PERSISTENT=0 runs them as one launch per step, replayed
+// from CUDA graphs in blocks of 4 iterations.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "ctx.h"
@@ -19,6 +23,9 @@ struct gbc_batch {
   gbc::LatCg* d_lat = nullptr;     // [n]: inner CG state per lattice
   int2* d_work = nullptr;
   int nwork = 0;
+  gbc::GridBar* d_bar = nullptr;     // grid barrier of the persistent kernel
+  gbc::PersistLat* d_pl = nullptr;   // [n]: reliable-update trigger state per lattice
+  int* d_pout = nullptr;             // iterations run by the last persistent launch
   std::string err;
 };
 
@@ -78,10 +85,9 @@ int gbc_batch_create(gbc_batch** out, int n, gbc_ctx* const* ctxs) {
   }
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc(&b->d_args, sizeof(HopArgs) * 4 * n) != cudaSuccess ||
-      cudaMalloc(&b->d_lat, sizeof(LatCg) * n) != cudaSuccess) {
-    if (b->d_args) cudaFree(b->d_args);
-    if (b->stream) cudaStreamDestroy(b->stream);
-    delete b;
+      cudaMalloc(&b->d_lat, sizeof(LatCg) * n) != cudaSuccess || cudaMalloc(&b->d_bar, sizeof(GridBar)) != cudaSuccess ||
+      cudaMalloc(&b->d_pl, sizeof(PersistLat) * n) != cudaSuccess || cudaMalloc(&b->d_pout, sizeof(int) * 2) != cudaSuccess) {
+    gbc_batch_destroy(b);
     return GBC_ERR_CUDA;
   }
   // work table: every 128-site block of every lattice, largest lattices first
@@ -94,10 +100,7 @@ int gbc_batch_create(gbc_batch** out, int n, gbc_ctx* const* ctxs) {
   b->nwork = (int)work.size();
   if (cudaMalloc(&b->d_work, sizeof(int2) * work.size()) != cudaSuccess ||
       cudaMemcpy(b->d_work, work.data(), sizeof(int2) * work.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
-    cudaFree(b->d_args);
-    cudaFree(b->d_lat);
-    cudaStreamDestroy(b->stream);
-    delete b;
+    gbc_batch_destroy(b);
     return GBC_ERR_CUDA;
   }
   *out = b;
@@ -110,6 +113,9 @@ void gbc_batch_destroy(gbc_batch* b) {
   if (b->d_args) cudaFree(b->d_args);
   if (b->d_lat) cudaFree(b->d_lat);
   if (b->d_work) cudaFree(b->d_work);
+  if (b->d_bar) cudaFree(b->d_bar);
+  if (b->d_pl) cudaFree(b->d_pl);
+  if (b->d_pout) cudaFree(b->d_pout);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -155,7 +161,7 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
     struct L {
       Spinor x, bd, rd, t1, t2, ted, rs, es, rhs, r, pv, mp, mmp, te, th1, teh;
       double bb = 0, rr = 0, prev_rr = HUGE_VAL;
-      int done = 0, iters = 0, outer = 0, status = GBC_OK;
+      int done = 0, iters = 0, outer = 0, reliable = 0, status = GBC_OK;
     };
     std::vector<L> lat(n);
     const size_t rs_can = 0;
@@ -200,6 +206,10 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
     }
     GBC_CUDA(cudaMemcpyAsync(b->d_args, args.data(), sizeof(HopArgs) * 4 * n, cudaMemcpyHostToDevice, s));
     const int recon = b->ctx[0]->pf[pidx(sloppy)].recon;
+    // the inner iterations as one persistent kernel per block of iterations (GBC_PERSISTENT=0: one
+    // launch per step, replayed from CUDA graphs)
+    const char* pe = getenv("GBC_PERSISTENT");
+    bool persist = !(pe && pe[0] == '0') && n <= kPersistMaxLattices && pa == S && sloppy != D;
     auto multi = [&](int k, int mode, bool dag, bool reduce) {
       if (hop_multi_launch(sloppy, recon, mode, dag, reduce, b->d_args + k * n, b->d_work, b->nwork, s) < 0)
         throw std::string("multi-lattice kernel variant not compiled");
@@ -300,14 +310,45 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
         GBC_CUDA(cudaMemcpyAsync(b->ctx[l]->d_cg, &st, sizeof(CGScalars), cudaMemcpyHostToDevice, s));
       }
       GBC_CUDA(cudaStreamSynchronize(s));
-      // first iteration uncaptured (tunes nothing: the multi kernel has one shape), then graph blocks
+      // The persistent kernel runs up to kPersistIters iterations per launch and stops by itself
+      // for a reliable update; otherwise the first iteration runs uncaptured, then graph blocks.
       constexpr int kBlock = 4;
+      constexpr int kPersistIters = 256;
       cudaGraphExec_t exec = nullptr;
       long long gl = 0;
       int k = 0;
       bool any = true;
       while (any && k < p.max_iter) {
-        if (k > 0 && b->ctx[0]->use_graphs) {
+        bool ran = false;
+        if (persist) {
+          std::vector<PersistLat> hp(n);
+          for (int l = 0; l < n; ++l) hp[l] = PersistLat{maxrr[l], at_update[l]};
+          GBC_CUDA(cudaMemcpyAsync(b->d_pl, hp.data(), sizeof(PersistLat) * n, cudaMemcpyHostToDevice, s));
+          const int kmax = std::min(kPersistIters, p.max_iter - k);
+          const int r = batch_cg_persistent(pa, sloppy, recon, b->d_args, b->d_lat, b->d_work, b->nwork, n, kmax,
+                                            p.delta, b->d_pl, b->d_bar, b->d_pout, s);
+          if (r > 0) GBC_CUDA((cudaError_t)r);
+          if (r < 0) {
+            persist = false;  // no persistent variant, or the cooperative launch was refused
+          } else {
+            GridBar hb{};
+            int ran_iters = 0;
+            GBC_CUDA(cudaMemcpyAsync(&hb, b->d_bar, sizeof(GridBar), cudaMemcpyDeviceToHost, s));
+            GBC_CUDA(cudaMemcpyAsync(&ran_iters, b->d_pout, sizeof(int), cudaMemcpyDeviceToHost, s));
+            GBC_CUDA(cudaMemcpyAsync(hp.data(), b->d_pl, sizeof(PersistLat) * n, cudaMemcpyDeviceToHost, s));
+            GBC_CUDA(cudaStreamSynchronize(s));
+            if (hb.err) {
+              if (exec) cudaGraphExecDestroy(exec);
+              throw std::string("persistent batch kernel: a grid-barrier wait gave up at barrier ") +
+                  std::to_string(hb.where);
+            }
+            for (int l = 0; l < n; ++l) maxrr[l] = hp[l].maxrr;
+            k += ran_iters;
+            ran = true;
+          }
+        }
+        if (ran) {
+        } else if (k > 0 && b->ctx[0]->use_graphs) {
           if (!exec) {
             cudaGraph_t graph;
             const long long c0 = launch_count();
@@ -347,6 +388,7 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
             gbc_ctx* c = b->ctx[l];
             L& q = lat[l];
             if (!hs[l].active) continue;
+            ++q.reliable;
             apply_meo(c, pa, false, q.es, q.th1, q.teh, false);
             apply_meo(c, pa, true, q.th1, q.r, q.teh, false);
             blas_xmy_norm2(c->g, q.rhs, q.r, red(c), s);
@@ -407,6 +449,7 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
       std::memset(&o, 0, sizeof(o));
       o.n_count = q.iters;
       o.n_outer = q.outer;
+      o.n_reliable = q.reliable;
       o.resid = std::sqrt(q.rr);
       o.rel_resid = q.bb > 0 ? std::sqrt(q.rr / q.bb) : o.resid;
       o.status = q.status != GBC_OK ? q.status : (q.done ? GBC_OK : GBC_ERR_NOT_CONVERGED);

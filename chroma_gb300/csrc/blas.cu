@@ -3,6 +3,8 @@
 // FP64: GB300's FP64 pipe made per-site FP64 sums the bottleneck of bandwidth-bound kernels), then
 // per-warp and per-block sums in FP64 in a fixed grid, then one deterministic finalize pass.  Also the device-side CG scalar logic, so that an iteration
 // needs no host round trip (InvCG2, lib/actions/ferm/invert/invcg2.cc:153-221).
+#include <string>
+
 #include "gbc_device.cuh"
 
 namespace gbc {
@@ -456,7 +458,26 @@ struct CloverF {
 };
 }  // namespace
 
-void blas_clover(const Geom& g, const void* clov, const Spinor& out, const Spinor& in, cudaStream_t s) {
+void blas_clover(const Geom& g, const void* clov, const Spinor& out, const Spinor& in, cudaStream_t s, bool df) {
+  if (df) {
+    if (in.prec != PREC_DOUBLE || out.prec != PREC_DOUBLE) throw std::string("double-float clover needs FP64 fields");
+    run<0>(g, in.nrhs, CloverF<PrecDF>{clov, out, in, g.stride}, nullptr, s);
+    return;
+  }
   GBC_DISPATCH1(in.prec, (run<0>(g, in.nrhs, CloverF<PA>{clov, out, in, g.stride}, nullptr, s)));
+}
+
+namespace {
+__global__ void split_kernel(const double* in, float2* out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const df64 v = df64_from_bits(in[i]);
+    out[i] = make_float2(v.hi, v.lo);
+  }
+}
+}  // namespace
+
+void split_df64(const double* in, float2* out, size_t n, cudaStream_t s) {
+  split_kernel<<<1216, 256, 0, s>>>(in, out, n);
+  count_launch();
 }
 }  // namespace gbc

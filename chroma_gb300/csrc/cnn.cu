@@ -207,7 +207,8 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], 
 }
 
 // out[b][j][o][a] = (G W^T)[row][2o + re/im] for every right-hand side b of the batch: the
-// weights and the block's transports are staged once, then per b the gathered tile G and its GEMM
+// weights and (for batches) the block's transports are staged once, then per b the gathered tile G
+// and its GEMM
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, int batch, const float2* links, const float2* hin,
                                                    float2* hout, const __nv_bfloat16* Wr) {
@@ -221,13 +222,17 @@ __global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, int batch, con
   for (int p = threadIdx.x; p < NP * KP; p += blockDim.x) W[(p / KP) * GP + p % KP] = Wr[p];
   tile_neighbours(nbr, g, V, site0);
   __syncthreads();
-  stage_transports(lk, nbr, V, links, site0);
+  // one right-hand side reads each transport once: it gathers straight from the links (the staged
+  // copy only costs shared memory and occupancy there)
+  const bool staged = batch > 1;
+  if (staged) stage_transports(lk, nbr, V, links, site0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int gid = lane >> 2, tig = lane & 3;
   constexpr int MT = ROWS / 16, NT = NP / 8;
   for (int b = 0; b < batch; ++b) {
     __syncthreads();  // transports staged; the previous right-hand side's GEMM is done with G
-    gather_tile_staged<CIN>(G, nbr, lk, V, hin + (size_t)b * V * CIN * 3, site0);
+    if (staged) gather_tile_staged<CIN>(G, nbr, lk, V, hin + (size_t)b * V * CIN * 3, site0);
+    else gather_tile<CIN>(G, nbr, V, links, hin + (size_t)b * V * CIN * 3, site0);
     __syncthreads();
     float2* out = hout + (size_t)b * V * COUT * 3;
     for (int t = warp; t < MT * NT; t += CT / 32) {
@@ -412,10 +417,12 @@ void launch_layer(const Geom& g, int V, int batch, const float2* links, const fl
                   const __nv_bfloat16* W, cudaStream_t s) {
   // tile G and weights W (bf16 at pitch gpitch; their bytes are a multiple of 8), then the staged
   // transports (float2)
-  const size_t smem = (size_t)(ROWS * gpitch(CIN) + npad(COUT) * gpitch(CIN)) * 2 + sizeof(float2) * SITES * 8 * 9;
+  const size_t tile = (size_t)(ROWS * gpitch(CIN) + npad(COUT) * gpitch(CIN)) * 2;
+  const size_t lkb = sizeof(float2) * SITES * 8 * 9;
+  const size_t smem = batch > 1 ? tile + lkb : tile;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(layer_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(layer_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(tile + lkb));
     attr = true;
   }
   dim3 grid((V + SITES - 1) / SITES);

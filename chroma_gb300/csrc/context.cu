@@ -103,6 +103,30 @@ void ensure_prec(gbc_ctx* c, int prec) {
   if (f.ready) return;
   if (!c->have_gauge) throw std::string("gauge field not loaded");
   const Geom& g = c->g;
+  if (prec == PREC_DF) {
+    // the FP64 links and clover with every double split into (hi, lo) floats, same layout
+    ensure_prec(c, PREC_DOUBLE);
+    const PrecFields& d = c->pf[pidx(PREC_DOUBLE)];
+    free_prec(f);
+    const size_t gb = gauge_plane_bytes(PREC_DOUBLE, 18) * g.stride;
+    for (int p = 0; p < 2; ++p)
+      for (int m = 0; m < 4; ++m) {
+        GBC_CUDA(cudaMalloc(&f.gauge[p][m], gb));
+        split_df64((const double*)d.gauge[p][m], (float2*)f.gauge[p][m], gb / 8, c->stream);
+      }
+    const size_t cb = clover_bytes(PREC_DOUBLE) * g.stride;
+    for (int p = 0; p < 2; ++p) {
+      GBC_CUDA(cudaMalloc(&f.clov[p], cb));
+      split_df64((const double*)d.clov[p], (float2*)f.clov[p], cb / 8, c->stream);
+    }
+    GBC_CUDA(cudaMalloc(&f.clovinv, cb));
+    split_df64((const double*)d.clovinv, (float2*)f.clovinv, cb / 8, c->stream);
+    GBC_CUDA(cudaGetLastError());
+    sync(c);
+    f.recon = 18;
+    f.ready = true;
+    return;
+  }
   int recon = prec == PREC_DOUBLE ? 18 : c->opts.sloppy_reconstruct;
   float* d_err = nullptr;
   GBC_CUDA(cudaMalloc(&d_err, sizeof(float)));
@@ -240,7 +264,8 @@ std::string default_tune_path() {
 }
 }  // namespace
 
-static int default_shape(int nrhs) {
+static int default_shape(int prec, int nrhs) {
+  if (prec == PREC_DF) return 0;  // the double-float kernels compile the one-site-per-thread shapes
   if (nrhs >= 12 && nrhs % 12 == 0) return 5;
   if (nrhs >= 4) return 3;
   return 1;
@@ -252,7 +277,7 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, int reduce,
       ((((long long)pidx(prec) * 4 + mode) * 2 + (dag ? 1 : 0)) * 3 + reduce) << 32 | (unsigned)h.nrhs;
   auto it = c->tuned.find(key);
   if (it != c->tuned.end()) return it->second;
-  int best = default_shape(h.nrhs);
+  int best = default_shape(prec, h.nrhs);
   // GBC_SHAPE=<index into kHopShapes> pins one shape (profiling); ignored when out of range
   if (const char* fs = getenv("GBC_SHAPE")) {
     const int si = atoi(fs);
@@ -405,7 +430,8 @@ void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& o
 void apply_clover(gbc_ctx* c, int prec, int parity, bool inverse, const Spinor& in, const Spinor& out) {
   if (inverse && parity == 1) ensure_sym(c, prec);
   const PrecFields& f = c->pf[pidx(prec)];
-  blas_clover(c->g, inverse ? (parity == 0 ? f.clovinv : f.clovinv_odd) : f.clov[parity], out, in, c->stream);
+  blas_clover(c->g, inverse ? (parity == 0 ? f.clovinv : f.clovinv_odd) : f.clov[parity], out, in, c->stream,
+              prec == PREC_DF);
   GBC_CUDA(cudaGetLastError());
 }
 
@@ -413,6 +439,14 @@ void ensure_sym(gbc_ctx* c, int prec) {
   ensure_prec(c, prec);
   PrecFields& f = c->pf[pidx(prec)];
   if (f.clovinv_odd) return;
+  if (prec == PREC_DF) {
+    ensure_sym(c, PREC_DOUBLE);
+    const size_t cb = clover_bytes(PREC_DOUBLE) * c->g.stride;
+    GBC_CUDA(cudaMalloc(&f.clovinv_odd, cb));
+    split_df64((const double*)c->pf[pidx(PREC_DOUBLE)].clovinv_odd, (float2*)f.clovinv_odd, cb / 8, c->stream);
+    GBC_CUDA(cudaGetLastError());
+    return;
+  }
   GBC_CUDA(cudaMalloc(&f.clovinv_odd, clover_bytes(prec) * c->g.stride));
   void* planes[2] = {nullptr, f.clovinv_odd};
   pack_clover(c->g, c->d_inv, prec, planes, 2, c->stream);
@@ -679,9 +713,11 @@ int gbc_get_logdet(gbc_ctx* c, double* logdet_even, double* logdet_odd) {
 int gbc_apply(gbc_ctx* c, int op, int isign, int cb, int prec, int nrhs, double* out, const double* in) {
   if (!c || !out || !in || nrhs < 1 || nrhs > c->max_rhs) return GBC_ERR_ARGS;
   if (isign != 1 && isign != -1) return GBC_ERR_ARGS;
-  if (prec != GBC_PREC_DOUBLE && prec != GBC_PREC_SINGLE && prec != GBC_PREC_HALF) return GBC_ERR_ARGS;
+  if (prec != GBC_PREC_DOUBLE && prec != GBC_PREC_SINGLE && prec != GBC_PREC_HALF && prec != GBC_PREC_DF64)
+    return GBC_ERR_ARGS;
   if (!c->have_gauge) return fail(c, GBC_ERR_STATE, "load the gauge field first");
   if (op < 0 || op > 7 || cb < 0 || cb > 1) return GBC_ERR_ARGS;
+  if (prec == GBC_PREC_DF64 && (op == GBC_OP_SYM || op == GBC_OP_SYM_MDAGM)) return GBC_ERR_ARGS;
   return guarded(c, [&]() {
     ensure_prec(c, prec);
     ensure_stage(c, nrhs);
@@ -691,10 +727,11 @@ int gbc_apply(gbc_ctx* c, int op, int isign, int cb, int prec, int nrhs, double*
     GBC_CUDA(cudaMemcpyAsync(c->d_stage[1], out, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     const bool dag = isign < 0;
     const PrecFields& f = c->pf[pidx(prec)];
-    Spinor a = sub(workspace(c, 100, prec, nrhs), 0, nrhs);
-    Spinor b = sub(workspace(c, 101, prec, nrhs), 0, nrhs);
-    Spinor t = sub(workspace(c, 102, prec, nrhs), 0, nrhs);
-    Spinor d = sub(workspace(c, 103, prec, nrhs), 0, nrhs);
+    const int sp = prec == GBC_PREC_DF64 ? GBC_PREC_DOUBLE : prec;  // storage of the spinors
+    Spinor a = sub(workspace(c, 100, sp, nrhs), 0, nrhs);
+    Spinor b = sub(workspace(c, 101, sp, nrhs), 0, nrhs);
+    Spinor t = sub(workspace(c, 102, sp, nrhs), 0, nrhs);
+    Spinor d = sub(workspace(c, 103, sp, nrhs), 0, nrhs);
     switch (op) {
       case GBC_OP_DSLASH:
         import_spinor(c->g, c->d_stage[0], rs, 1 - cb, a, c->stream);

@@ -15,7 +15,10 @@
 
 namespace gbc {
 
-inline int pidx(int prec) { return prec == PREC_DOUBLE ? 0 : prec == PREC_SINGLE ? 1 : 2; }
+// index of a precision's device fields in gbc_ctx::pf (PREC_DF: the double-float split copies)
+inline int pidx(int prec) {
+  return prec == PREC_DOUBLE ? 0 : prec == PREC_SINGLE ? 1 : prec == PREC_HALF ? 2 : 3;
+}
 
 struct PrecFields {
   bool ready = false;
@@ -57,7 +60,7 @@ struct gbc_ctx {
   double logdet_odd = 0;   // the same over the odd sites
   int nneg = 0;
 
-  gbc::PrecFields pf[3];
+  gbc::PrecFields pf[4];  // FP64, FP32, FP16 fields and the double-float copies of the FP64 ones
 
   // reductions and CG scalars
   int max_rhs = 12;

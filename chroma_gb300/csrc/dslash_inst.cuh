@@ -19,12 +19,21 @@ static int hop_shape(const HopArgs& a, HopShape sh, cudaStream_t s) {
 #define GBC_SHAPE(TX, NRB, MINB)                                 \
   if (!sh.pair && sh.tx == TX && sh.nrb == NRB && sh.minb == MINB) \
     return go(hop_kernel<P, RECON, MODE, DAG, REDUCE, TX, NRB, MINB>, TX, NRB);
-  GBC_SHAPE(128, 1, 1)
-  GBC_SHAPE(128, 1, 6)
-  GBC_SHAPE(32, 4, 1)
-  GBC_SHAPE(32, 4, 5)
-  GBC_SHAPE(64, 2, 4)
-  GBC_SHAPE(32, 12, 2)
+  if constexpr (std::is_same<P, PrecDF>::value) {
+    // double-float arithmetic: about ten times the instructions of the FP32 kernel, so only the
+    // shapes without a tight register bound
+    GBC_SHAPE(128, 1, 1)
+    GBC_SHAPE(32, 4, 1)
+    GBC_SHAPE(64, 2, 4)
+    return -1;
+  } else {
+    GBC_SHAPE(128, 1, 1)
+    GBC_SHAPE(128, 1, 6)
+    GBC_SHAPE(32, 4, 1)
+    GBC_SHAPE(32, 4, 5)
+    GBC_SHAPE(64, 2, 4)
+    GBC_SHAPE(32, 12, 2)
+  }
 #undef GBC_SHAPE
   if constexpr (std::is_same<P, PrecH>::value) {
     if (sh.pair == 3) {
@@ -72,7 +81,26 @@ static int hop_shape(const HopArgs& a, HopShape sh, cudaStream_t s) {
 }
 
 template <typename P, int RECON, bool DAG>
+static int hop_mode_reduce(int mode, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
+
+template <typename P, int RECON, bool DAG>
 static int hop_mode(int mode, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
+  if constexpr (std::is_same<P, PrecDF>::value) {
+    // the outer residuals and the Schur prep apply the operator without fused reductions
+    if (reduce) return -1;
+    switch (mode) {
+      case HOP_PLAIN: return hop_shape<P, RECON, HOP_PLAIN, DAG, RED_NONE>(a, sh, s);
+      case HOP_CLOV: return hop_shape<P, RECON, HOP_CLOV, DAG, RED_NONE>(a, sh, s);
+      case HOP_XPAY: return hop_shape<P, RECON, HOP_XPAY, DAG, RED_NONE>(a, sh, s);
+    }
+    return -1;
+  } else {
+    return hop_mode_reduce<P, RECON, DAG>(mode, reduce, a, sh, s);
+  }
+}
+
+template <typename P, int RECON, bool DAG>
+static int hop_mode_reduce(int mode, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s) {
   switch (mode) {
     case HOP_PLAIN: return reduce ? -1 : hop_shape<P, RECON, HOP_PLAIN, DAG, RED_NONE>(a, sh, s);
     case HOP_CLOV: return reduce ? -1 : hop_shape<P, RECON, HOP_CLOV, DAG, RED_NONE>(a, sh, s);

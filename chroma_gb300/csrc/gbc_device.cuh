@@ -15,6 +15,8 @@
 //           double : double2 [36][stride]
 //           single : float4  [18][stride]
 //           half   : per block uint4[4] + uint2[1]  -> uint4 [8][stride] then uint2 [2][stride]
+//   double-float copies of the FP64 links and clover (PrecDF): the FP64 planes with every double
+//   split into (hi, lo) floats, a double2 (re, im) becoming a float4 (re.hi, re.lo, im.hi, im.lo)
 #pragma once
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -97,11 +99,101 @@ __device__ __forceinline__ int full_index(const Geom& g, const Coord& c) {
 }
 
 // --------------------------------------------------------------------------------------------
+// Double-float arithmetic: a value is hi + lo with two floats (a 48-bit significand), built from
+// the error-free transformations TwoSum (Knuth), QuickTwoSum (Dekker) and TwoProduct by FMA, in the
+// "sloppy" addition of the published double-double libraries (Bailey's DD, Hida-Li-Bailey QD):
+// the error of a sum is of the order 2^-46 of its largest operand.  GB300 runs FP32 at many times
+// its FP64 rate, so FP64-stored fields go through stencils in this arithmetic where ~1e-14 of
+// accuracy suffices.  Every operation uses the _rn intrinsics, which the compiler never contracts
+// into FMAs (contraction would break the error-free transformations).
+// --------------------------------------------------------------------------------------------
+struct df64 {
+  float hi, lo;
+  df64() = default;
+  __device__ __forceinline__ df64(float h, float l) : hi(h), lo(l) {}
+  __device__ __forceinline__ df64(int v) : hi((float)v), lo(0.f) {}
+  __device__ __forceinline__ df64(float v) : hi(v), lo(0.f) {}
+  __device__ __forceinline__ df64(double v);
+};
+
+__device__ __forceinline__ df64 quick_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return df64(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ df64 two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float v = __fsub_rn(s, a);
+  return df64(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v)));
+}
+__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
+  const df64 s = two_sum(a.hi, b.hi);
+  return quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
+__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
+__device__ __forceinline__ df64 operator*(df64 a, df64 b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return quick_two_sum(p, e);
+}
+__device__ __forceinline__ df64& operator+=(df64& a, df64 b) { return a = a + b; }
+// a * b + c with one renormalisation
+__device__ __forceinline__ df64 fmadd(df64 a, df64 b, df64 c) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const df64 s = two_sum(p, c.hi);
+  return quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(e, c.lo)));
+}
+
+// double -> hi + lo by integer operations (GB300's FP64 pipe, which the conversion instructions
+// would use, is the slow part this arithmetic avoids): hi = the leading 24 bits of the significand,
+// lo = the remaining 29 bits rounded to 24, then renormalised.  |x| below 2^-126 maps to zero (far
+// below any field value the solvers carry); |x| above float's range is not a lattice field value.
+__device__ __forceinline__ df64 df64_from_bits(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e < 897) return df64(0.f, 0.f);
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  const float hi = __uint_as_float(sgn | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29));
+  const unsigned ml = (unsigned)(m & 0x1FFFFFFFull);
+  float lo = 0.f;
+  if (e >= 949) {
+    // ml = mh 2^23 + mlow with both parts exact in float (magic-number conversion), then one rounding
+    const float mlow = __fsub_rn(__uint_as_float(0x4B000000u | (ml & 0x7FFFFFu)), 8388608.f);
+    const float mh = __fsub_rn(__uint_as_float(0x4B000000u | (ml >> 23)), 8388608.f);
+    const float mf = __fmaf_rn(mh, 8388608.f, mlow);
+    lo = __uint_as_float(__float_as_uint(__fmul_rn(mf, __uint_as_float((unsigned)(e - 948) << 23))) | sgn);
+  }
+  return quick_two_sum(hi, lo);
+}
+__device__ __forceinline__ df64::df64(double v) { *this = df64_from_bits(v); }
+
+// float -> double by integer operations (exact; zero and subnormal floats map to zero)
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0) return 0.0;
+  const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ double df64_to_double(df64 v) { return f2d_bits(v.hi) + f2d_bits(v.lo); }
+
+// --------------------------------------------------------------------------------------------
 // Precision tags
 // --------------------------------------------------------------------------------------------
 struct PrecD { using real = double; static constexpr int bytes = 8; };
 struct PrecS { using real = float; static constexpr int bytes = 4; };
 struct PrecH { using real = float; static constexpr int bytes = 2; };  // fp16 storage, fp32 arithmetic
+// FP64 storage, double-float arithmetic: spinors are the FP64 fields; links and clover come from
+// a copy whose every FP64 value is split once into (hi, lo) floats (same bytes, same plane layout,
+// a double2 (re, im) becoming a float4 (re.hi, re.lo, im.hi, im.lo))
+struct PrecDF { using real = df64; static constexpr int bytes = 8; };
 
 // Accumulator of a site functor's reductions: F::Acc when the functor declares one (its compute
 // precision), else double.  The reduction drivers sum a thread's sites and the lanes of a warp in
@@ -120,6 +212,7 @@ template <typename P> struct Store;
 template <> struct Store<PrecD> { using vec = double2; };
 template <> struct Store<PrecS> { using vec = float4; };
 template <> struct Store<PrecH> { using vec = uint4; };
+template <> struct Store<PrecDF> { using vec = double2; };
 
 // Spinor views: base pointer of one right-hand side, plus norm for half
 template <typename P>
@@ -137,8 +230,17 @@ __device__ __forceinline__ uint32_t f2h(float a, float b) {
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
+#ifdef GBC_COHERENT_LOADS
+// Translation units whose kernels read fields that other blocks of the same launch wrote (the
+// persistent batch kernel, between its grid barriers): plain loads, which the barrier's gpu-scope
+// fences order after those writes.  The read-only path (ld.global.nc) requires data that no one
+// writes while the kernel runs.
+template <typename T>
+__device__ __forceinline__ T ldg(const T* p) { return *p; }
+#else
 template <typename T>
 __device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
+#endif
 
 // ---- spinor load/store -------------------------------------------------------------------------
 template <typename P>
@@ -182,9 +284,28 @@ __device__ __forceinline__ void load_spinor<PrecH>(cplx<float> (&s)[12], const v
   }
 }
 
+template <>
+__device__ __forceinline__ void load_spinor<PrecDF>(cplx<df64> (&s)[12], const void* base, const float*, int idx,
+                                                    int stride) {
+  const double2* p = reinterpret_cast<const double2*>(base);
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    double2 v = ldg(p + (size_t)k * stride + idx);
+    s[k] = {df64_from_bits(v.x), df64_from_bits(v.y)};
+  }
+}
+
 template <typename P>
 __device__ __forceinline__ void store_spinor(void* base, float* norm, int idx, int stride,
                                              const cplx<typename P::real> (&s)[12]);
+template <>
+__device__ __forceinline__ void store_spinor<PrecDF>(void* base, float*, int idx, int stride,
+                                                     const cplx<df64> (&s)[12]) {
+  double2* p = reinterpret_cast<double2*>(base);
+#pragma unroll
+  for (int k = 0; k < 12; ++k)
+    p[(size_t)k * stride + idx] = make_double2(df64_to_double(s[k].re), df64_to_double(s[k].im));
+}
 
 template <>
 __device__ __forceinline__ void store_spinor<PrecD>(void* base, float*, int idx, int stride,
@@ -233,12 +354,14 @@ template <> struct LinkPlanes<PrecS, 18> { static constexpr int n = 5; };
 template <> struct LinkPlanes<PrecS, 12> { static constexpr int n = 3; };
 template <> struct LinkPlanes<PrecH, 18> { static constexpr int n = 5; };
 template <> struct LinkPlanes<PrecH, 12> { static constexpr int n = 3; };
+template <> struct LinkPlanes<PrecDF, 18> { static constexpr int n = 9; };
 
 template <typename P>
 struct LinkVec;
 template <> struct LinkVec<PrecD> { using vec = double2; };
 template <> struct LinkVec<PrecS> { using vec = float4; };
 template <> struct LinkVec<PrecH> { using vec = uint2; };
+template <> struct LinkVec<PrecDF> { using vec = float4; };
 
 // Load link (row-major 3x3) from its planes; for RECON 12 rebuild row 2 = sign * conj(row0 x row1).
 template <typename P, int RECON>
@@ -252,6 +375,14 @@ __device__ __forceinline__ void load_link(cplx<typename P::real> (&u)[9], const 
     for (int k = 0; k < NC; ++k) {
       double2 v = ldg(p + (size_t)k * stride + idx);
       u[k] = {v.x, v.y};
+    }
+  } else if constexpr (std::is_same<P, PrecDF>::value) {
+    static_assert(RECON == 18, "FP64-stored links keep 18 reals");
+    const float4* p = reinterpret_cast<const float4*>(base);
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      float4 v = ldg(p + (size_t)k * stride + idx);
+      u[k] = {df64(v.x, v.y), df64(v.z, v.w)};
     }
   } else if constexpr (std::is_same<P, PrecS>::value) {
     const float4* p = reinterpret_cast<const float4*>(base);
@@ -297,6 +428,19 @@ __device__ __forceinline__ void load_clover_block(typename P::real (&d)[6], cplx
     for (int k = 0; k < 15; ++k) {
       double2 v = ldg(p + (size_t)(3 + k) * stride);
       o[k] = {v.x, v.y};
+    }
+  } else if constexpr (std::is_same<P, PrecDF>::value) {
+    const float4* p = reinterpret_cast<const float4*>(base) + (size_t)(18 * b) * stride + idx;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float4 v = ldg(p + (size_t)k * stride);
+      d[2 * k] = df64(v.x, v.y);
+      d[2 * k + 1] = df64(v.z, v.w);
+    }
+#pragma unroll
+    for (int k = 0; k < 15; ++k) {
+      float4 v = ldg(p + (size_t)(3 + k) * stride);
+      o[k] = {df64(v.x, v.y), df64(v.z, v.w)};
     }
   } else if constexpr (std::is_same<P, PrecS>::value) {
     const float4* p = reinterpret_cast<const float4*>(base) + (size_t)(9 * b) * stride + idx;

@@ -15,6 +15,9 @@ enum { HOP_PLAIN = 0, HOP_CLOV = 1, HOP_XPAY = 2 };
 // epilogue (BiCGStab's (t, s), (t, t) for t = M~ s), three partial rows per right-hand side
 enum { RED_NONE = 0, RED_NORM = 1, RED_DOT_SELF = 2 };
 enum { PREC_HALF = 2, PREC_SINGLE = 4, PREC_DOUBLE = 8 };
+// internal arithmetic mode, not a storage precision: FP64-stored fields, double-float arithmetic
+// (the PrecDF kernels on the split copies of the FP64 links and clover)
+enum { PREC_DF = 16 };
 
 struct Geom {
   int L[4];
@@ -118,9 +121,11 @@ inline int hop_multi_launch(int prec, int recon, int mode, bool dag, int reduce,
   return -1;
 }
 
+int hop_launch_df(int recon, int mode, bool dag, int reduce, const HopArgs& a, HopShape sh, cudaStream_t s);
 inline int hop_launch(int prec, int recon, int mode, bool dag, int reduce, const HopArgs& a, HopShape sh,
                       cudaStream_t s) {
   switch (prec) {
+    case PREC_DF: return hop_launch_df(recon, mode, dag, reduce, a, sh, s);
     case PREC_DOUBLE: return hop_launch_d(recon, mode, dag, reduce, a, sh, s);
     case PREC_SINGLE: return hop_launch_s(recon, mode, dag, reduce, a, sh, s);
     case PREC_HALF: return hop_launch_h(recon, mode, dag, reduce, a, sh, s);
@@ -215,9 +220,40 @@ void batch_cg_update(int pa, int po, const LatCg* lat, const int2* work, int nwo
 void batch_cg_beta(const LatCg* lat, int n, cudaStream_t s);
 void batch_xpay(int pa, int po, const LatCg* lat, const int2* work, int nwork, cudaStream_t s);
 
+// ---- the same iterations as one persistent kernel (batch_persistent.cuh) -----------------------
+// Software grid barrier of a cooperative launch: arrival counter, generation, error flag (a wait
+// that gave up).  Zeroed before every launch.
+struct GridBar {
+  unsigned count;
+  unsigned gen;
+  int err;
+  int where;  // barrier index of the first wait that gave up
+};
+// per lattice: the largest |r| since the last reliable update and |r| at that update (the
+// reliable-update trigger of the host loop), read and written back by the kernel
+struct PersistLat {
+  double maxrr, at_update;
+};
+constexpr int kPersistMaxLattices = 32;
+// Runs up to kmax CGNE iterations of every active lattice in one cooperative launch (grid = the
+// co-resident blocks, at most nwork): the four stencil passes, the update and p = r + b p walk the
+// work table, alpha and beta are summed by every block from the partials (identical sums in every
+// block, so no scalar is shared), 6 grid barriers per iteration.  Stops when no lattice is active,
+// or after an iteration (every fourth of the launch) in which an active lattice's |r| fell below
+// delta * maxrr or rose above at_update (a reliable update is due); writes the CGScalars and PersistLat back and
+// out[0] = iterations run.  Returns 0, -1 when (pa, po, recon) has no persistent variant or the
+// cooperative launch is refused (the caller then uses the per-launch path), or the CUDA error.
+int batch_cg_persistent(int pa, int po, int recon, const HopArgs* args, const LatCg* lat, const int2* work,
+                        int nwork, int n, int kmax, double delta, PersistLat* pl, GridBar* bar, int* out,
+                        cudaStream_t s);
+
 }  // namespace gbc
 
 namespace gbc {
 // out = T in (T = packed clover blocks of the field's parity, prec of the spinors)
-void blas_clover(const Geom& g, const void* clov, const Spinor& out, const Spinor& in, cudaStream_t s);
+// (df: FP64 spinors, clover as the double-float split copy, double-float arithmetic)
+void blas_clover(const Geom& g, const void* clov, const Spinor& out, const Spinor& in, cudaStream_t s,
+                 bool df = false);
+// out[i] = (hi, lo) floats of in[i]: the double-float copy of an FP64 field (n doubles)
+void split_df64(const double* in, float2* out, size_t n, cudaStream_t s);
 }  // namespace gbc

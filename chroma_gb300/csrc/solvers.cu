@@ -10,8 +10,9 @@
 //                           FP64 residual and solves for the correction with a CGNE whose operator
 //                           and search vectors are in the sloppy precision and whose residual is
 //                           refreshed from an FP32 operator (reliable updates)
-//   GBC_SOLVER_FGMRES       FGMRES(NKrylov), NDefl = 0 (fgmres below), optionally preconditioned by
-//                           the learned network (precond.cu), inside the same FP64 defect correction
+//   GBC_SOLVER_FGMRES       FGMRES-DR(NKrylov, NDefl) (fgmres below; NDefl = 0 is plain restarted
+//                           FGMRES), optionally preconditioned by the learned network (precond.cu),
+//                           inside the same FP64 defect correction
 //   GBC_SOLVER_BICGSTAB     the same FP64 defect correction around a reliable BiCGStab on M~
 //                           (bicgstab.cu; RELIABLE_BICGSTAB_MP_CLOVER_INVERTER, reliable_bicgstab.cc:
 //                           18-277); MdagM systems, and the rest of a solve whose inner BiCGStab broke
@@ -21,6 +22,7 @@
 // side keeps alpha = beta = 0 so that the batch can run on until the last one converges.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include <complex>
@@ -397,6 +399,10 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
     }
   };
   auto put_coef = [&](const std::vector<cd>& cf, int rows) {  // cf[row * n + rhs]
+    // the staging buffer is pinned, so the copy reads it when the stream reaches it: wait for the
+    // previous copy from it before overwriting (the deflated restart and the final x += Z eta
+    // upload coefficients back to back)
+    sync(c);
     for (size_t k = 0; k < cf.size(); ++k) c->h_kcoef[k] = make_double2(cf[k].real(), cf[k].imag());
     GBC_CUDA(cudaMemcpyAsync(c->d_kcoef, c->h_kcoef, sizeof(double2) * rows * n, cudaMemcpyHostToDevice, s));
   };
@@ -467,7 +473,7 @@ CgStats fgmres(gbc_ctx* c, int pa, int po, const Spinor& x, const Spinor& b, dou
       }
       if (gg == 0.0) {
         ss = 0.0;
-        cc = std::conj(f) / std::abs(f);
+        cc = f / std::abs(f);  // rot() maps f to conj(cc) f = |f|
         return std::abs(f);
       }
       const double t = std::sqrt(std::norm(f) + std::norm(gg));
@@ -774,6 +780,13 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     ensure_prec(c, sloppy);
     ensure_prec(c, PREC_SINGLE);
   }
+  // The Schur prep and the intermediate residuals of the defect correction run in double-float
+  // arithmetic on the FP64 fields (about 1e-14 relative, far below any target): GB300 executes
+  // FP32 at a large multiple of its FP64 rate.  The solution's reconstruction and the final true
+  // residual stay FP64.  GBC_OUTER_DF=0 (and the symmetric operator) keeps every step in FP64.
+  const char* odf = getenv("GBC_OUTER_DF");
+  const int DX = (odf && odf[0] == '0') || symmetric ? D : PREC_DF;
+  if (DX == PREC_DF) ensure_prec(c, PREC_DF);
   if (symmetric) {
     // A_oo^-1 packed before any iteration is captured into a graph
     ensure_sym(c, D);
@@ -803,8 +816,8 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     psie = sub(workspace(c, SLOT_PSIE, D, n), 0, n);
     import_spinor(g, chi_canon, rs, 0, chie, s);
     std::vector<double> no = norm2(c, chi), ne = norm2(c, chie);
-    apply_clover(c, D, 0, true, chie, ted);
-    hop(c, D, 1, HOP_PLAIN, false, 0.5, ted, t1, nullptr, nullptr, false);
+    apply_clover(c, DX, 0, true, chie, ted);
+    hop(c, DX, 1, HOP_PLAIN, false, 0.5, ted, t1, nullptr, nullptr, false);
     blas_xpy(g, chi, t1, s);
     // the even reconstruction is exact, so the full residual equals the odd one: solve the odd
     // system to target * |chi| / |chi'_o| so that |M psi - chi| / |chi| meets the target
@@ -924,10 +937,10 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
         blas_norm2(g, rd, red(c), s);
         rr_exact = false;
       } else {
-        // FP64 residual
-        apply_sys(c, D, mdagm, psi, rd, t2, ted);
+        // residual with the FP64 fields (double-float arithmetic unless GBC_OUTER_DF=0)
+        apply_sys(c, DX, mdagm, psi, rd, t2, ted);
         blas_xmy_norm2(g, chi, rd, red(c), s);
-        rr_exact = true;
+        rr_exact = DX == D;
       }
       std::vector<double> rr = fetch(c, 1, n);
       // A correction that left the FP64 residual larger than before (an inner solve that broke

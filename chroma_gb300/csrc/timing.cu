@@ -55,16 +55,19 @@ extern "C" int gbc_time_operator(gbc_ctx* c, int op, int prec, int nrhs, int ite
     c->err = "no learned preconditioner loaded";
     return GBC_ERR_PRECOND;
   }
-  if (prec != GBC_PREC_DOUBLE && prec != GBC_PREC_SINGLE && prec != GBC_PREC_HALF) return GBC_ERR_ARGS;
+  if (prec != GBC_PREC_DOUBLE && prec != GBC_PREC_SINGLE && prec != GBC_PREC_HALF && prec != GBC_PREC_DF64)
+    return GBC_ERR_ARGS;
+  if (prec == GBC_PREC_DF64 && op == GBC_TIME_PRECOND) return GBC_ERR_ARGS;
+  const int sp = prec == GBC_PREC_DF64 ? GBC_PREC_DOUBLE : prec;  // storage of the fields
   if (!c->have_gauge) {
     c->err = "load the gauge field first";
     return GBC_ERR_STATE;
   }
   try {
     ensure_prec(c, prec);
-    Spinor in = sub(workspace(c, 200, prec, nrhs), 0, nrhs);
-    Spinor out = sub(workspace(c, 201, prec, nrhs), 0, nrhs);
-    Spinor te = sub(workspace(c, 202, prec, nrhs), 0, nrhs);
+    Spinor in = sub(workspace(c, 200, sp, nrhs), 0, nrhs);
+    Spinor out = sub(workspace(c, 201, sp, nrhs), 0, nrhs);
+    Spinor te = sub(workspace(c, 202, sp, nrhs), 0, nrhs);
     fill(c, in, 12345u);
     fill(c, out, 777u);
     uint4* junk = nullptr;
@@ -97,7 +100,7 @@ extern "C" int gbc_time_operator(gbc_ctx* c, int op, int prec, int nrhs, int ite
     *seconds = total / iters;
     if (bytes) {
       const PrecFields& f = c->pf[pidx(prec)];
-      double L = link_bytes(prec, f.recon), S = spinor_bytes(prec), Cb = clover_site_bytes(prec);
+      double L = link_bytes(sp, f.recon), S = spinor_bytes(sp), Cb = clover_site_bytes(sp);
       double Vh = c->g.Vh;
       if (op == GBC_TIME_PRECOND) {
         // per layer: the FP32 links of every site once, the FP32 activations in and out of every

@@ -18,6 +18,7 @@ ERRORS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "solver did not co
           5: "non-finite value", 6: "invalid call order", 7: "12-real reconstruction not possible",
           8: "learned preconditioner unavailable"}
 PREC_HALF, PREC_SINGLE, PREC_DOUBLE = 2, 4, 8
+PREC_DF64 = 16  # operator arithmetic of apply / time_operator: FP64 fields, double-float arithmetic
 RECON_18, RECON_12 = 18, 12
 OP_DSLASH, OP_CLOVER, OP_CLOVINV, OP_MEO, OP_MDAGM, OP_UNPREC, OP_SYM, OP_SYM_MDAGM = range(8)
 TIME_PRECOND = 100  # gbc_time_operator: one application of the learned preconditioner

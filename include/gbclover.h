@@ -43,6 +43,10 @@ extern "C" {
 #define GBC_PREC_HALF 2
 #define GBC_PREC_SINGLE 4
 #define GBC_PREC_DOUBLE 8
+/* operator arithmetic of gbc_apply and gbc_time_operator only (not a storage precision): the FP64
+   fields in double-float arithmetic (two floats per value, ~48-bit significand), the arithmetic of
+   the solvers' Schur prep and intermediate defect-correction residuals */
+#define GBC_PREC_DF64 16
 /* gauge reconstruction: RECONS_NONE = 18 reals, RECONS_12 */
 #define GBC_RECON_18 18
 #define GBC_RECON_12 12
@@ -177,7 +181,8 @@ int gbc_get_logdet(gbc_ctx* ctx, double* logdet_even, double* logdet_odd);
 /* ---- operators (parity tests; LinearOperator<LatticeFermion>::operator(), lib/linearop.h:25-49) */
 /* out/in: nrhs host spinors (full lattice); only the parity the operator reads/writes matters;
    sites of the other parity in out are left untouched.  prec selects the storage precision
-   the operator runs in (GBC_PREC_DOUBLE for the FP64 path). */
+   the operator runs in (GBC_PREC_DOUBLE for the FP64 path), or GBC_PREC_DF64 (not for the
+   symmetric operators). */
 int gbc_apply(gbc_ctx* ctx, int op, int isign, int cb, int prec, int nrhs, double* out, const double* in);
 
 /* ---- BLAS-1 (parity tests of the reductions and fused updates the solvers run) -------------- */

@@ -1,5 +1,6 @@
-"""Batched solves of independent lattices of uneven size (one multi-lattice stencil launch per
-application), checked lattice by lattice with the CPU oracle: FP64 true residual <= 1e-10."""
+"""Batched solves of independent lattices of uneven size (one multi-lattice stencil pass per
+application), checked lattice by lattice with the CPU oracle: FP64 true residual <= 1e-10, for the
+persistent kernel (GBC_PERSISTENT=1, the default) and the one-launch-per-step path."""
 import numpy as np
 import pytest
 
@@ -9,7 +10,9 @@ from chroma_gb300 import sources as S
 pytestmark = pytest.mark.gpu
 
 
-def test_batch_of_uneven_lattices():
+@pytest.mark.parametrize("persistent", ["1", "0"], ids=["persistent", "graphs"])
+def test_batch_of_uneven_lattices(persistent, monkeypatch):
+    monkeypatch.setenv("GBC_PERSISTENT", persistent)
     from oracle import Oracle, OracleOp
     from oracle import oracle as O
     o = Oracle()
@@ -72,3 +75,41 @@ def test_tight_target_below_inner_precision(sloppy):
         assert bres[0]["status"] == 0
     finally:
         ctx.close()
+
+
+def test_persistent_kernel_matches_per_launch_path(monkeypatch):
+    """The persistent kernel runs the same recursion as the per-launch path: the same solutions (to
+    the FP64 target), iteration counts within a few per lattice (the reliable-update tests fall on
+    every fourth iteration of a launch, not of the solve), and far fewer launches."""
+    kappa, csw = 0.124, 1.5
+    mass = 1 / (2 * kappa) - 4
+    lattices = [(8, 8, 8, 16), (4, 4, 4, 8), (12, 12, 12, 24)]
+    ctxs, chis = [], []
+    for k, dims in enumerate(lattices):
+        c = G.Context(dims, mass, csw, t_boundary=-1, max_rhs=1)
+        c.load_gauge(G.gauge_synthetic(dims, 0.3, 900 + k, t_boundary=-1))
+        ctxs.append(c)
+        chis.append(S.z2_noise(dims, 950 + k, cb=1).reshape(-1, 12))
+    batch = G.Batch(ctxs)
+    try:
+        out = {}
+        for mode in ("1", "0"):
+            monkeypatch.setenv("GBC_PERSISTENT", mode)
+            psis, res = batch.solve(chis, rsd_target=1e-10)
+            assert all(r["status"] == 0 and r["rel_resid"] <= 1e-10 for r in res), res
+            out[mode] = (psis, res)
+        for k in range(len(lattices)):
+            a, b = out["1"][0][k], out["0"][0][k]
+            assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-8
+            ia, ib = out["1"][1][k]["n_count"], out["0"][1][k]["n_count"]
+            print(f"{lattices[k]}: iterations {ia} / {ib}, reliable updates {out['1'][1][k]['n_reliable']} / "
+                  f"{out['0'][1][k]['n_reliable']}, outer steps {out['1'][1][k]['n_outer']} / "
+                  f"{out['0'][1][k]['n_outer']} (persistent / per-launch)")
+            assert abs(ia - ib) <= max(8, 0.1 * ib), (lattices[k], ia, ib)
+        la, lb = out["1"][1][0]["launches"], out["0"][1][0]["launches"]
+        print(f"launches per batch solve: persistent {la}, per-launch {lb}")
+        assert la * 2 < lb, (la, lb)
+    finally:
+        batch.close()
+        for c in ctxs:
+            c.close()
