@@ -17,8 +17,9 @@
 // host reports the solve as failed; no wait is unbounded.  A cooperative launch guarantees that
 // every block is resident, so the barrier is only a guard against the unexpected.
 //
-// This file is compiled with GBC_COHERENT_LOADS (plain loads instead of ld.global.nc): the fields
-// read after a barrier were written by other blocks of the same launch.
+// This file is compiled with GBC_COHERENT_LOADS: spinor fields, which other blocks of the same
+// launch wrote before a barrier, are read with plain loads instead of ld.global.nc (links and
+// clover, which nothing writes, keep the read-only path).
 #pragma once
 #include <algorithm>
 
@@ -53,7 +54,7 @@ __device__ __forceinline__ bool grid_barrier(GridBar* gb, unsigned nblocks, int 
           good = 0;
           break;
         }
-        __nanosleep(100);
+        __nanosleep(32);
       }
     }
     __threadfence();

@@ -145,17 +145,17 @@ __device__ __forceinline__ void load_spinor_f2(float2 (&s)[12], float& n, const 
     const float4* p = reinterpret_cast<const float4*>(base);
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-      float4 v = ldg(p + (size_t)k * stride + idx);
+      float4 v = ldw(p + (size_t)k * stride + idx);
       s[2 * k] = make_float2(v.x, v.y);
       s[2 * k + 1] = make_float2(v.z, v.w);
     }
     n = 1.0f;
   } else {
     const uint4* p = reinterpret_cast<const uint4*>(base);
-    n = ldg(norm + idx);
+    n = ldw(norm + idx);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      uint4 v = ldg(p + (size_t)k * stride + idx);
+      uint4 v = ldw(p + (size_t)k * stride + idx);
       s[4 * k + 0] = h2f(v.x);
       s[4 * k + 1] = h2f(v.y);
       s[4 * k + 2] = h2f(v.z);
@@ -273,13 +273,13 @@ __device__ __forceinline__ void load_project_h(float2 (&h)[2][3], float& n, cons
   uint32_t w[12];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const uint4 v = ldg(p + (size_t)k * stride + idx);
+    const uint4 v = ldw(p + (size_t)k * stride + idx);
     w[4 * k] = v.x;
     w[4 * k + 1] = v.y;
     w[4 * k + 2] = v.z;
     w[4 * k + 3] = v.w;
   }
-  n = ldg(norm + idx);
+  n = ldw(norm + idx);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     __half2 a, b;

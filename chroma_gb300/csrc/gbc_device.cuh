@@ -230,16 +230,19 @@ __device__ __forceinline__ uint32_t f2h(float a, float b) {
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
-#ifdef GBC_COHERENT_LOADS
-// Translation units whose kernels read fields that other blocks of the same launch wrote (the
-// persistent batch kernel, between its grid barriers): plain loads, which the barrier's gpu-scope
-// fences order after those writes.  The read-only path (ld.global.nc) requires data that no one
-// writes while the kernel runs.
-template <typename T>
-__device__ __forceinline__ T ldg(const T* p) { return *p; }
-#else
+// Loads of data that no kernel writes while it runs (links, clover, tables): the read-only path.
 template <typename T>
 __device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
+// Loads of spinor fields and their norms.  Translation units whose kernels read fields that other
+// blocks of the same launch wrote (the persistent batch kernel, between its grid barriers) define
+// GBC_COHERENT_LOADS: plain loads, which the barrier's gpu-scope fences order after those writes;
+// the read-only path (ld.global.nc) requires data that no one writes while the kernel runs.
+#ifdef GBC_COHERENT_LOADS
+template <typename T>
+__device__ __forceinline__ T ldw(const T* p) { return *p; }
+#else
+template <typename T>
+__device__ __forceinline__ T ldw(const T* p) { return __ldg(p); }
 #endif
 
 // ---- spinor load/store -------------------------------------------------------------------------
@@ -253,7 +256,7 @@ __device__ __forceinline__ void load_spinor<PrecD>(cplx<double> (&s)[12], const 
   const double2* p = reinterpret_cast<const double2*>(base);
 #pragma unroll
   for (int k = 0; k < 12; ++k) {
-    double2 v = ldg(p + (size_t)k * stride + idx);
+    double2 v = ldw(p + (size_t)k * stride + idx);
     s[k] = {v.x, v.y};
   }
 }
@@ -263,7 +266,7 @@ __device__ __forceinline__ void load_spinor<PrecS>(cplx<float> (&s)[12], const v
   const float4* p = reinterpret_cast<const float4*>(base);
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
-    float4 v = ldg(p + (size_t)k * stride + idx);
+    float4 v = ldw(p + (size_t)k * stride + idx);
     s[2 * k] = {v.x, v.y};
     s[2 * k + 1] = {v.z, v.w};
   }
@@ -272,10 +275,10 @@ template <>
 __device__ __forceinline__ void load_spinor<PrecH>(cplx<float> (&s)[12], const void* base, const float* norm, int idx,
                                                    int stride) {
   const uint4* p = reinterpret_cast<const uint4*>(base);
-  float n = ldg(norm + idx);
+  float n = ldw(norm + idx);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    uint4 v = ldg(p + (size_t)k * stride + idx);
+    uint4 v = ldw(p + (size_t)k * stride + idx);
     float2 a = h2f(v.x), b = h2f(v.y), c = h2f(v.z), d = h2f(v.w);
     s[4 * k + 0] = {a.x * n, a.y * n};
     s[4 * k + 1] = {b.x * n, b.y * n};
@@ -290,7 +293,7 @@ __device__ __forceinline__ void load_spinor<PrecDF>(cplx<df64> (&s)[12], const v
   const double2* p = reinterpret_cast<const double2*>(base);
 #pragma unroll
   for (int k = 0; k < 12; ++k) {
-    double2 v = ldg(p + (size_t)k * stride + idx);
+    double2 v = ldw(p + (size_t)k * stride + idx);
     s[k] = {df64_from_bits(v.x), df64_from_bits(v.y)};
   }
 }
