@@ -31,14 +31,22 @@ namespace persistent {
 
 constexpr long long kWaitCycles = 4000000000LL;  // SM clock cycles (~2 s at 2 GHz)
 
-// returns false when this barrier or an earlier one of the launch gave up waiting
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// returns false when this barrier or an earlier one of the launch gave up waiting.  Arrival is a
+// release-ordered atomic on the counter; the last block resets it and bumps the generation, which
+// the others poll with acquire loads (busy for the first polls, then with short sleeps); the error
+// flag and the clock are looked at every 64 polls only.
 __device__ __forceinline__ bool grid_barrier(GridBar* gb, unsigned nblocks, int where) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned* genp = &gb->gen;
     volatile int* errp = &gb->err;
-    const unsigned g = *genp;
+    const unsigned g = ld_acquire(&gb->gen);
     __threadfence();
     const unsigned arrived = atomicAdd(&gb->count, 1u) + 1u;
     int good = 1;
@@ -48,13 +56,13 @@ __device__ __forceinline__ bool grid_barrier(GridBar* gb, unsigned nblocks, int 
       atomicAdd(&gb->gen, 1u);
     } else {
       const long long t0 = clock64();
-      while (*genp == g) {
-        if (*errp || clock64() - t0 > kWaitCycles) {
+      for (unsigned polls = 1; ld_acquire(&gb->gen) == g; ++polls) {
+        if ((polls & 63) == 0 && (*errp || clock64() - t0 > kWaitCycles)) {
           if (atomicCAS(&gb->err, 0, 1) == 0) gb->where = where;
           good = 0;
           break;
         }
-        __nanosleep(32);
+        if (polls > 256) __nanosleep(20);
       }
     }
     __threadfence();
@@ -81,8 +89,8 @@ __device__ __forceinline__ double block_total(const double* part, int n) {
   return t;
 }
 
-template <typename PA, typename PO, int RECON>
-__global__ void __launch_bounds__(kBatchSites, 4)
+template <typename PA, typename PO, int RECON, int MINB>
+__global__ void __launch_bounds__(kBatchSites, MINB)
 cg_kernel(const HopArgs* __restrict__ args, const LatCg* __restrict__ lat, const int2* __restrict__ work, int nwork,
           int n, int kmax, double delta, PersistLat* pl, GridBar* gb, int* out) {
   constexpr int L = kPersistMaxLattices;
@@ -208,10 +216,10 @@ cg_kernel(const HopArgs* __restrict__ args, const LatCg* __restrict__ lat, const
   }
 }
 
-template <typename PA, typename PO, int RECON>
+template <typename PA, typename PO, int RECON, int MINB = 4>
 int launch(const HopArgs* args, const LatCg* lat, const int2* work, int nwork, int n, int kmax, double delta,
            PersistLat* pl, GridBar* bar, int* out, cudaStream_t s) {
-  auto kern = cg_kernel<PA, PO, RECON>;
+  auto kern = cg_kernel<PA, PO, RECON, MINB>;
   static int per_sm = -1, sms = 0;
   if (per_sm < 0) {
     int dev = 0;

@@ -1,6 +1,6 @@
 """Batched solves of independent lattices of uneven size (one multi-lattice stencil pass per
 application), checked lattice by lattice with the CPU oracle: FP64 true residual <= 1e-10, for the
-persistent kernel (GBC_PERSISTENT=1, the default) and the one-launch-per-step path."""
+one-launch-per-step path (the default) and the persistent kernel (GBC_PERSISTENT=1)."""
 import numpy as np
 import pytest
 
