@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--dims", default=None, help="override lattice, e.g. 16,16,16,32 (testing only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1)
-    ap.add_argument("--op-only", default=None, choices=["dslash16", "dslash32", "dslash64", "meo16", "meo64"],
+    ap.add_argument("--op-only", default=None,
+                    choices=["dslash16", "dslash32", "dslash64", "meo16", "meo64", "meodf", "dslashdf"],
                     help="profiling mode: set up the workload and time one operator only")
     ap.add_argument("--nrhs", type=int, default=12)
     ap.add_argument("--recon", type=int, default=12, choices=[12, 18])
@@ -76,7 +77,8 @@ def op_only(args):
     ctx.load_gauge(links)
     op, prec = {"dslash16": (G.OP_DSLASH, G.PREC_HALF), "dslash32": (G.OP_DSLASH, G.PREC_SINGLE),
                 "dslash64": (G.OP_DSLASH, G.PREC_DOUBLE), "meo16": (G.OP_MEO, G.PREC_HALF),
-                "meo64": (G.OP_MEO, G.PREC_DOUBLE)}[args.op_only]
+                "meo64": (G.OP_MEO, G.PREC_DOUBLE), "meodf": (G.OP_MEO, G.PREC_DF64),
+                "dslashdf": (G.OP_DSLASH, G.PREC_DF64)}[args.op_only]
     sec, byts = ctx.time_operator(op, prec, nrhs=args.nrhs, iters=args.iters, flush_l2=True)
     if args.profile_timed:
         # a second, tuned run inside cudaProfilerStart/Stop (ncu --profile-from-start off)
@@ -497,6 +499,27 @@ def main():
     last = results[-1]
     psi_host = psi_d.cpu().numpy().view(np.complex128).reshape(nsrc, V, 12)
 
+    # e2e through the public API with pinned host buffers, right after the device-timed steps
+    chi_h = torch.from_numpy(src.view(np.float64).copy()).pin_memory()
+    psi_h = torch.zeros_like(chi_h).pin_memory()
+    e2e_t, e2e_dev = [], []
+    import ctypes as C
+    p = G.SolveParams(G.SOLVER_BICGSTAB, G.SYS_FULL, RSD, 10000, DELTA, 10.0, G.PREC_HALF, INNER_TOL, 0, 16, 0, 1)
+    # the same K steps as the device-timed loop, each through gbc_solve with pinned host buffers
+    for i in range(args.steps):
+        flush.random_()
+        torch.cuda.synchronize()
+        res_arr = (G.Result * nsrc)()
+        t0 = time.perf_counter()
+        rc = ctx.lib.gbc_solve(ctx.h, C.byref(p), nsrc, C.cast(psi_h.data_ptr(), C.POINTER(C.c_double)),
+                               C.cast(chi_h.data_ptr(), C.POINTER(C.c_double)), res_arr)
+        e2e_t.append(time.perf_counter() - t0)
+        e2e_dev.append(res_arr[0].device_seconds)
+        if rc != 0:
+            raise RuntimeError("e2e solve failed")
+    e2e = max_over_ranks(sum(e2e_t) / len(e2e_t), world) / world
+    nbytes = src.nbytes
+
     # plain FP64 CG on the same GPU, sources one at a time (quarkProp4_a's loop)
     plain, plain_iters, plain_res, err_vs_fp64 = None, [], [None], None
     if args.plain_steps > 0:
@@ -579,26 +602,6 @@ def main():
             "single_rhs_fp64_gbs": byts64 / sec64 / 1e9,
             "meo_12rhs_fp64_s": m64, "meo_12rhs_double_float_s": mdf}
 
-    # e2e through the public API with pinned host buffers
-    chi_h = torch.from_numpy(src.view(np.float64).copy()).pin_memory()
-    psi_h = torch.zeros_like(chi_h).pin_memory()
-    e2e_t, e2e_dev = [], []
-    import ctypes as C
-    p = G.SolveParams(G.SOLVER_BICGSTAB, G.SYS_FULL, RSD, 10000, DELTA, 10.0, G.PREC_HALF, INNER_TOL, 0, 16, 0, 1)
-    # the same K steps as the device-timed loop, each through gbc_solve with pinned host buffers
-    for i in range(args.steps):
-        flush.random_()
-        torch.cuda.synchronize()
-        res_arr = (G.Result * nsrc)()
-        t0 = time.perf_counter()
-        rc = ctx.lib.gbc_solve(ctx.h, C.byref(p), nsrc, C.cast(psi_h.data_ptr(), C.POINTER(C.c_double)),
-                               C.cast(chi_h.data_ptr(), C.POINTER(C.c_double)), res_arr)
-        e2e_t.append(time.perf_counter() - t0)
-        e2e_dev.append(res_arr[0].device_seconds)
-        if rc != 0:
-            raise RuntimeError("e2e solve failed")
-    e2e = max_over_ranks(sum(e2e_t) / len(e2e_t), world) / world
-    nbytes = src.nbytes
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and plain_iters:

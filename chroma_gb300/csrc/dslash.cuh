@@ -96,6 +96,64 @@ __device__ __forceinline__ void adj_mat_vec2(cplx<T> (&uh)[2][3], const cplx<T> 
     }
 }
 
+// Double-float colour products with one renormalisation per output component: the exact products
+// of the high parts are summed by TwoSum and their rounding errors, with the cross terms, in a plain
+// float (the compensated dot product Dot2 of Ogita, Rump and Oishi, SIAM J. Sci. Comput. 26, 2005):
+// 12 FP32 operations per product instead of 15, and a shorter dependency chain.
+struct Dot2 {
+  float s, c;
+};
+__device__ __forceinline__ void dot2_add(Dot2& d, df64 a, df64 b) {  // d += a b
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const df64 t = two_sum(d.s, p);
+  d.s = t.hi;
+  d.c = __fadd_rn(d.c, __fadd_rn(t.lo, e));
+}
+__device__ __forceinline__ df64 dot2_value(const Dot2& d) { return quick_two_sum(d.s, d.c); }
+
+template <>
+__device__ __forceinline__ void mat_vec2<df64>(cplx<df64> (&uh)[2][3], const cplx<df64> (&u)[9],
+                                              const cplx<df64> (&h)[2][3]) {
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      Dot2 re{0.f, 0.f}, im{0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const cplx<df64> x = u[3 * r + k], y = h[s][k];
+        dot2_add(re, x.re, y.re);
+        dot2_add(re, -x.im, y.im);
+        dot2_add(im, x.re, y.im);
+        dot2_add(im, x.im, y.re);
+      }
+      uh[s][r] = {dot2_value(re), dot2_value(im)};
+    }
+}
+
+template <>
+__device__ __forceinline__ void adj_mat_vec2<df64>(cplx<df64> (&uh)[2][3], const cplx<df64> (&u)[9],
+                                                  const cplx<df64> (&h)[2][3]) {
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      Dot2 re{0.f, 0.f}, im{0.f, 0.f};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const cplx<df64> x = u[3 * k + r], y = h[s][k];  // conj(u[k][r]) h[k]
+        dot2_add(re, x.re, y.re);
+        dot2_add(re, x.im, y.im);
+        dot2_add(im, x.re, y.im);
+        dot2_add(im, -x.im, y.re);
+      }
+      uh[s][r] = {dot2_value(re), dot2_value(im)};
+    }
+}
+
 template <typename P, int RECON, int MU, bool DAG>
 __device__ __forceinline__ void hop_dir(cplx<typename P::real> (&acc)[12], const HopArgs& a, const Coord& c, int idx,
                                         const char* in, const float* in_norm) {
