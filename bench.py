@@ -39,7 +39,7 @@ RSD = 1e-10
 DELTA = 0.01  # reliable-update threshold of the inner BiCGStab (the XML's Delta)
 INNER_TOL = 1e-5  # inner relative tolerance of each outer step (the XML's InnerTol)
 # InvCG2 iterations sampled per timed step of the CPU legs (bounded samples of the full solve)
-CPU_SAMPLE_ITERS = 12
+CPU_SAMPLE_ITERS = 20
 # ncu DRAM bytes (read + write) of one 12-RHS FP16 M~ (its two stencil launches) at 24^3x48
 M12_TRAFFIC_24 = 1228.1e6
 

@@ -780,12 +780,14 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     ensure_prec(c, sloppy);
     ensure_prec(c, PREC_SINGLE);
   }
-  // The Schur prep and the intermediate residuals of the defect correction run in double-float
-  // arithmetic on the FP64 fields (about 1e-14 relative, far below any target): GB300 executes
-  // FP32 at a large multiple of its FP64 rate.  The solution's reconstruction and the final true
-  // residual stay FP64.  GBC_OUTER_DF=0 (and the symmetric operator) keeps every step in FP64.
+  // For the full system, the Schur prep and the intermediate residuals of the defect correction
+  // run in double-float arithmetic on the FP64 fields (about 1e-14 relative, far below any
+  // target): GB300 executes FP32 at a large multiple of its FP64 rate.  The solution's
+  // reconstruction and the final true residual stay FP64.  The odd-site systems keep FP64
+  // residuals, whose last one is also their final check; GBC_OUTER_DF=0 (and the symmetric
+  // operator) keeps every step in FP64.
   const char* odf = getenv("GBC_OUTER_DF");
-  const int DX = (odf && odf[0] == '0') || symmetric ? D : PREC_DF;
+  const int DX = (odf && odf[0] == '0') || symmetric || p.system != GBC_SYS_FULL ? D : PREC_DF;
   if (DX == PREC_DF) ensure_prec(c, PREC_DF);
   if (symmetric) {
     // A_oo^-1 packed before any iteration is captured into a graph
