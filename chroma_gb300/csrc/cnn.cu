@@ -8,13 +8,15 @@
 //
 // W acts on channels only and the links on colour only, so every layer (and the network) is
 // gauge covariant.  The channel mixing is a GEMM over the rows (site, colour): the gathered
-// T_d h form a 9*C_in complex row, staged in shared memory as BF16, and mma.sync m16n8k16
-// (BF16 in, FP32 accumulate) multiplies it by the real form of W.  The network is linear; it
-// takes the odd-site input as channels = spins with zero even sites and returns its odd sites.
+// T_d h form a 9*C_in complex row, staged in shared memory as BF16 in the tensor cores' core-matrix
+// layout, and tcgen05.mma (BF16 in, FP32 accumulate in tensor memory) multiplies it by the real
+// form of W.  The network is linear; it takes the odd-site input as channels = spins with zero
+// even sites and returns its odd sites.
 //
 // Backward: the input gradient of a layer is the same layer with W'_{+mu} = W_{-mu}^H,
 // W'_{-mu} = W_{+mu}^H, W'_0 = W_0^H (T_{+mu}^dag = T_{-mu}), and the weight gradient is
-// sum over rows of delta_out (x) conj(gathered input), also on the tensor cores.
+// sum over rows of delta_out (x) conj(gathered input), with mma.sync m16n8k16 (a reduction over
+// the rows into a small matrix, accumulated across blocks with atomics).
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -62,6 +64,23 @@ __host__ __device__ constexpr int gpitch(int cin) {
   return kpad(cin) + ((4 - (kpad(cin) / 2) % 8 + 8) % 8) * 2;
 }
 
+// Where element (row, k) of a staged bf16 tile lives, in elements from the tile base:
+//  - PitchLayout: row-major at pitch gpitch(cin) (the mma.sync fragments of the weight gradient);
+//  - CoreLayout: the tensor cores' canonical K-major layout without swizzle, read by tcgen05.mma
+//    through a shared-memory descriptor: 8 x 8 core matrices (8 rows of 16 bytes, 128 contiguous
+//    bytes), the core matrices of a row group along K 128 bytes apart (the descriptor's leading
+//    byte offset), row groups KP * 16 bytes apart (its stride byte offset).
+template <int CIN>
+struct PitchLayout {
+  __device__ __forceinline__ int operator()(int row, int k) const { return row * gpitch(CIN) + k; }
+};
+template <int CIN>
+struct CoreLayout {
+  __device__ __forceinline__ int operator()(int row, int k) const {
+    return (row >> 3) * (kpad(CIN) * 8) + (k >> 3) * 64 + (row & 7) * 8 + (k & 7);
+  }
+};
+
 // the 9 sites each site of the tile reads (d = 0 itself, 1 + 2 mu forward, 2 + 2 mu backward)
 __device__ void tile_neighbours(int (*nbr)[9], const Geom& g, int V, int site0) {
   for (int p = threadIdx.x; p < SITES * 9; p += blockDim.x) {
@@ -82,26 +101,27 @@ __device__ void tile_neighbours(int (*nbr)[9], const Geom& g, int V, int site0) 
 // padding zeroed.  One task per (site, direction, channel), channel fastest: consecutive threads
 // read consecutive channel vectors and write consecutive 32-bit words (re, im packed), and the
 // link of a (site, direction) is shared through L1 by the threads of its channels.
-template <int CIN>
+template <int CIN, class Lay>
 __device__ void gather_tile(__nv_bfloat16* G, const int (*nbr)[9], int V, const float2* links, const float2* h,
-                            int site0) {
-  constexpr int GP = gpitch(CIN);
+                            int site0, Lay lay) {
   for (int p = threadIdx.x; p < SITES * 9 * CIN; p += blockDim.x) {
     const int i = p % CIN, sd = p / CIN, s = sd % SITES, d = sd / SITES;
     const int j = site0 + s;
-    uint32_t* row = reinterpret_cast<uint32_t*>(G + (size_t)(s * 3) * GP + (d * CIN + i) * 2);
-    constexpr int RW = GP / 2;  // pitch in 32-bit words
+    const int k = (d * CIN + i) * 2;
+    auto put = [&](int a, uint32_t v) { *reinterpret_cast<uint32_t*>(G + lay(s * 3 + a, k)) = v; };
     if (j >= V) {
-      row[0] = row[RW] = row[2 * RW] = 0u;
+      put(0, 0u);
+      put(1, 0u);
+      put(2, 0u);
       continue;
     }
     const int n = nbr[s][d];
     const float2* src = h + ((size_t)n * CIN + i) * 3;
     const float2 x0 = src[0], x1 = src[1], x2 = src[2];
     if (d == 0) {
-      row[0] = bf16x2(x0.x, x0.y);
-      row[RW] = bf16x2(x1.x, x1.y);
-      row[2 * RW] = bf16x2(x2.x, x2.y);
+      put(0, bf16x2(x0.x, x0.y));
+      put(1, bf16x2(x1.x, x1.y));
+      put(2, bf16x2(x2.x, x2.y));
       continue;
     }
     const int mu = (d - 1) >> 1;
@@ -122,7 +142,7 @@ __device__ void gather_tile(__nv_bfloat16* G, const int (*nbr)[9], int V, const 
       }
       const float re = u0.x * x0.x - u0.y * x0.y + u1.x * x1.x - u1.y * x1.y + u2.x * x2.x - u2.y * x2.y;
       const float im = u0.x * x0.y + u0.y * x0.x + u1.x * x1.y + u1.y * x1.x + u2.x * x2.y + u2.y * x2.x;
-      row[a * RW] = bf16x2(re, im);
+      put(a, bf16x2(re, im));
     }
   }
   // zero the K padding
@@ -130,7 +150,7 @@ __device__ void gather_tile(__nv_bfloat16* G, const int (*nbr)[9], int V, const 
   if (KP > K)
     for (int p = threadIdx.x; p < ROWS * (KP - K); p += blockDim.x) {
       const int r = p / (KP - K), k = K + p % (KP - K);
-      G[(size_t)r * GP + k] = __float2bfloat16(0.f);
+      G[lay(r, k)] = __float2bfloat16(0.f);
     }
 }
 
@@ -154,25 +174,26 @@ __device__ void stage_transports(float2 (*lk)[8][9], const int (*nbr)[9], int V,
 // G as gather_tile, from staged transports: one task per (site, direction, channel), channel
 // fastest, so that consecutive threads read consecutive channel vectors of a neighbour and write
 // consecutive words of a row; the transport comes from shared memory instead of the links.
-template <int CIN>
+template <int CIN, class Lay>
 __device__ void gather_tile_staged(__nv_bfloat16* G, const int (*nbr)[9], const float2 (*lk)[8][9], int V,
-                                   const float2* h, int site0) {
-  constexpr int GP = gpitch(CIN);
-  constexpr int RW = GP / 2;  // pitch in 32-bit words
+                                   const float2* h, int site0, Lay lay) {
   for (int p = threadIdx.x; p < SITES * 9 * CIN; p += blockDim.x) {
     const int i = p % CIN, sd = p / CIN, s = sd % SITES, d = sd / SITES;
     const int j = site0 + s;
-    uint32_t* row = reinterpret_cast<uint32_t*>(G + (size_t)(s * 3) * GP + (d * CIN + i) * 2);
+    const int k = (d * CIN + i) * 2;
+    auto put = [&](int a, uint32_t v) { *reinterpret_cast<uint32_t*>(G + lay(s * 3 + a, k)) = v; };
     if (j >= V) {
-      row[0] = row[RW] = row[2 * RW] = 0u;
+      put(0, 0u);
+      put(1, 0u);
+      put(2, 0u);
       continue;
     }
     const float2* src = h + ((size_t)nbr[s][d] * CIN + i) * 3;
     const float2 x0 = src[0], x1 = src[1], x2 = src[2];
     if (d == 0) {
-      row[0] = bf16x2(x0.x, x0.y);
-      row[RW] = bf16x2(x1.x, x1.y);
-      row[2 * RW] = bf16x2(x2.x, x2.y);
+      put(0, bf16x2(x0.x, x0.y));
+      put(1, bf16x2(x1.x, x1.y));
+      put(2, bf16x2(x2.x, x2.y));
       continue;
     }
     const float2* m = lk[s][d - 1];
@@ -181,7 +202,7 @@ __device__ void gather_tile_staged(__nv_bfloat16* G, const int (*nbr)[9], const 
       const float2 u0 = m[3 * a], u1 = m[3 * a + 1], u2 = m[3 * a + 2];
       const float re = u0.x * x0.x - u0.y * x0.y + u1.x * x1.x - u1.y * x1.y + u2.x * x2.x - u2.y * x2.y;
       const float im = u0.x * x0.y + u0.y * x0.x + u1.x * x1.y + u1.y * x1.x + u2.x * x2.y + u2.y * x2.x;
-      row[a * RW] = bf16x2(re, im);
+      put(a, bf16x2(re, im));
     }
   }
   // zero the K padding
@@ -189,7 +210,7 @@ __device__ void gather_tile_staged(__nv_bfloat16* G, const int (*nbr)[9], const 
   if (KP > K)
     for (int p = threadIdx.x; p < ROWS * (KP - K); p += blockDim.x) {
       const int r = p / (KP - K), k = K + p % (KP - K);
-      G[(size_t)r * GP + k] = __float2bfloat16(0.f);
+      G[lay(r, k)] = __float2bfloat16(0.f);
     }
 }
 
@@ -206,58 +227,161 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// ---- 5th-generation tensor cores (tcgen05) for the forward channel mixing ----------------------
+// One thread issues tcgen05.mma (kind::f16, BF16 in, FP32 accumulate in tensor memory) on
+// shared-memory descriptors of the gathered tile G (128 rows: the block's 96 (site, colour) rows
+// plus zero padding) and the weights W (NU rows = output channels x re/im, padded to a multiple
+// of 16); completion is signalled through an mbarrier by tcgen05.commit, and each warp reads its
+// 32 accumulator lanes back with tcgen05.ld.
+
+__device__ int g_tc_wait_errors;  // waits for tensor-core completion that gave up (host-checked)
+
+// shared-memory matrix descriptor, K-major without swizzle: start, leading byte offset (between
+// K-adjacent core matrices), stride byte offset (between 8-row groups), descriptor version 1
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, N and M
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// thread 0 waits for phase `parity` of the mbarrier, for about 1 s of SM clock at most
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > 2000000000LL) return false;
+  }
+}
+
+template <int NU>
+__device__ __forceinline__ void tmem_load_row(uint32_t taddr, float (&v)[NU]) {
+  uint32_t r[NU];
+  if constexpr (NU == 32) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+  } else {
+    static_assert(NU == 16, "16 or 32 accumulator columns");
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+  }
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < NU; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+__host__ __device__ constexpr int nump(int cout) { return ((2 * cout + 15) / 16) * 16; }  // N of the MMA
+constexpr int kTmemCols = 32;  // tensor-memory columns allocated per block (>= nump, power of 2)
+
 // out[b][j][o][a] = (G W^T)[row][2o + re/im] for every right-hand side b of the batch: the
 // weights and (for batches) the block's transports are staged once, then per b the gathered tile G
-// and its GEMM
+// and its GEMM on the tensor cores
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, int batch, const float2* links, const float2* hin,
                                                    float2* hout, const __nv_bfloat16* Wr) {
-  constexpr int KP = kpad(CIN), NP = npad(COUT), GP = gpitch(CIN);
-  extern __shared__ __align__(16) unsigned char smem[];
-  __nv_bfloat16* G = reinterpret_cast<__nv_bfloat16*>(smem);
-  __nv_bfloat16* W = G + ROWS * GP;  // same pitch: the B fragment loads are conflict-free too
-  float2(*lk)[8][9] = reinterpret_cast<float2(*)[8][9]>(W + NP * GP);
+  constexpr int KP = kpad(CIN), NP = npad(COUT), NU = nump(COUT);
+  constexpr int MROWS = 128;  // the MMA's M: the 96 rows of the tile padded with zero rows
+  static_assert(ROWS <= MROWS && NU <= kTmemCols, "tile does not fit the MMA");
+  extern __shared__ __align__(128) unsigned char smem[];
+  __nv_bfloat16* G = reinterpret_cast<__nv_bfloat16*>(smem);  // CoreLayout, MROWS x KP
+  __nv_bfloat16* W = G + MROWS * KP;                          // CoreLayout, NU x KP
+  float2(*lk)[8][9] = reinterpret_cast<float2(*)[8][9]>(W + NU * KP);
   __shared__ int nbr[SITES][9];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int s_ok;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int site0 = blockIdx.x * SITES;
-  for (int p = threadIdx.x; p < NP * KP; p += blockDim.x) W[(p / KP) * GP + p % KP] = Wr[p];
+  const CoreLayout<CIN> lay{};
+  for (int p = tid; p < NU * KP; p += blockDim.x) {
+    const int n = p / KP, k = p % KP;
+    W[lay(n, k)] = n < NP ? Wr[(size_t)n * KP + k] : __float2bfloat16(0.f);
+  }
+  for (int p = tid; p < (MROWS - ROWS) * KP; p += blockDim.x) G[ROWS * KP + p] = __float2bfloat16(0.f);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
   tile_neighbours(nbr, g, V, site0);
   __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base;
   // one right-hand side reads each transport once: it gathers straight from the links (the staged
   // copy only costs shared memory and occupancy there)
   const bool staged = batch > 1;
   if (staged) stage_transports(lk, nbr, V, links, site0);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int gid = lane >> 2, tig = lane & 3;
-  constexpr int MT = ROWS / 16, NT = NP / 8;
-  for (int b = 0; b < batch; ++b) {
-    __syncthreads();  // transports staged; the previous right-hand side's GEMM is done with G
-    if (staged) gather_tile_staged<CIN>(G, nbr, lk, V, hin + (size_t)b * V * CIN * 3, site0);
-    else gather_tile<CIN>(G, nbr, V, links, hin + (size_t)b * V * CIN * 3, site0);
+  const uint64_t adesc = umma_desc(smem_u32(G), 128, KP * 16);
+  const uint64_t bdesc = umma_desc(smem_u32(W), 128, KP * 16);
+  constexpr uint32_t idesc = umma_idesc_bf16(MROWS, NU);
+  bool ok = true;
+  for (int b = 0; b < batch && ok; ++b) {
+    __syncthreads();  // transports staged; the previous right-hand side's accumulators are read
+    if (staged) gather_tile_staged<CIN>(G, nbr, lk, V, hin + (size_t)b * V * CIN * 3, site0, lay);
+    else gather_tile<CIN>(G, nbr, V, links, hin + (size_t)b * V * CIN * 3, site0, lay);
+    // the tensor cores read G through the async proxy
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     __syncthreads();
-    float2* out = hout + (size_t)b * V * COUT * 3;
-    for (int t = warp; t < MT * NT; t += CT / 32) {
-      const int mt = t % MT, nt = t / MT;
-      float c[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int ks = 0; ks < KP / 16; ++ks) {
-        const __nv_bfloat16* A0 = G + (size_t)(mt * 16 + gid) * GP + ks * 16 + 2 * tig;
-        const __nv_bfloat16* A1 = A0 + 8 * GP;
-        uint32_t a[4] = {ld_bf16x2(A0), ld_bf16x2(A1), ld_bf16x2(A0 + 8), ld_bf16x2(A1 + 8)};
-        const __nv_bfloat16* B0 = W + (size_t)(nt * 8 + gid) * GP + ks * 16 + 2 * tig;
-        uint32_t bb[2] = {ld_bf16x2(B0), ld_bf16x2(B0 + 8)};
-        mma_bf16(c, a, bb);
-      }
-      const int o = nt * 4 + tig;
-      if (o < COUT) {
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-          const int row = mt * 16 + gid + 8 * half;
-          const int s = row / 3, a = row % 3;
-          const int j = site0 + s;
-          if (j < V) out[((size_t)j * COUT + o) * 3 + a] = make_float2(c[2 * half], c[2 * half + 1]);
-        }
+      for (int ks = 0; ks < KP / 16; ++ks) {
+        // K steps of 16 elements: two core matrices along K, 256 bytes
+        const uint64_t da = adesc + (uint64_t)((ks * 256) >> 4), db = bdesc + (uint64_t)((ks * 256) >> 4);
+        const uint32_t acc = ks > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       smem_u32(&mbar))
+                   : "memory");
+      s_ok = mbar_wait(smem_u32(&mbar), (uint32_t)(b & 1));
+      if (!s_ok) atomicAdd(&g_tc_wait_errors, 1);
+    }
+    __syncthreads();
+    ok = s_ok != 0;
+    if (!ok) break;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const int row = warp * 32 + lane;
+    if (warp * 32 < ROWS) {  // warp 3 holds only padding rows
+      float v[NU];
+      tmem_load_row<NU>(tmem + ((uint32_t)(warp * 32) << 16), v);
+      const int s = row / 3, a = row % 3, j = site0 + s;
+      if (row < ROWS && j < V) {
+        float2* out = hout + (size_t)b * V * COUT * 3;
+#pragma unroll
+        for (int o = 0; o < COUT; ++o) out[((size_t)j * COUT + o) * 3 + a] = make_float2(v[2 * o], v[2 * o + 1]);
       }
     }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   }
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
 }
 
 // gradient of the real-form weights: dW[n][k] += sum_rows delta[row][n] * G[row][k]
@@ -273,7 +397,7 @@ __global__ void __launch_bounds__(CT) wgrad_kernel(Geom g, int V, const float2* 
   const int site0 = blockIdx.x * SITES;
   tile_neighbours(nbr, g, V, site0);
   __syncthreads();
-  gather_tile<CIN>(G, nbr, V, links, hin + (size_t)b * V * CIN * 3, site0);
+  gather_tile<CIN>(G, nbr, V, links, hin + (size_t)b * V * CIN * 3, site0, PitchLayout<CIN>{});
   const float2* dl = delta + (size_t)b * V * COUT * 3;
   for (int p = threadIdx.x; p < MP * ROWS; p += blockDim.x) {
     const int n = p / ROWS, row = p % ROWS;
@@ -415,9 +539,9 @@ __global__ void links_kernel(Geom g, int V, const double2* canon, float2* links)
 template <int CIN, int COUT>
 void launch_layer(const Geom& g, int V, int batch, const float2* links, const float2* in, float2* out,
                   const __nv_bfloat16* W, cudaStream_t s) {
-  // tile G and weights W (bf16 at pitch gpitch; their bytes are a multiple of 8), then the staged
-  // transports (float2)
-  const size_t tile = (size_t)(ROWS * gpitch(CIN) + npad(COUT) * gpitch(CIN)) * 2;
+  // tile G (128 rows) and weights W (nump rows), bf16 in the tensor cores' core-matrix layout
+  // (their bytes are a multiple of 128), then the staged transports (float2)
+  const size_t tile = (size_t)(128 * kpad(CIN) + nump(COUT) * kpad(CIN)) * 2;
   const size_t lkb = sizeof(float2) * SITES * 8 * 9;
   const size_t smem = batch > 1 ? tile + lkb : tile;
   static bool attr = false;
@@ -585,6 +709,19 @@ void Cnn::forward(gbc_ctx* c, int batch) {
   for (int l = 0; l < nlayers; ++l) layer(c->g, V, batch, cin(l), cout(l), links, act[l], act[l + 1], dW[l], c->stream);
 }
 
+// A layer whose wait for its tensor-core results gave up (it then frees its tensor memory and
+// returns) counts in g_tc_wait_errors: read and reset it, and fail the call that ran the layers.
+static void check_tc_waits(cudaStream_t s) {
+  int n = 0;
+  GBC_CUDA(cudaMemcpyFromSymbolAsync(&n, g_tc_wait_errors, sizeof(int), 0, cudaMemcpyDeviceToHost, s));
+  GBC_CUDA(cudaStreamSynchronize(s));
+  if (n) {
+    const int zero = 0;
+    GBC_CUDA(cudaMemcpyToSymbol(g_tc_wait_errors, &zero, sizeof(int)));
+    throw std::string("network layer: a wait for the tensor cores gave up");
+  }
+}
+
 double Cnn::loss_and_grad(gbc_ctx* c, int batch, const float2* target, const double* enorm2) {
   const int V = (int)c->V;
   cudaStream_t s = c->stream;
@@ -609,6 +746,7 @@ double Cnn::loss_and_grad(gbc_ctx* c, int batch, const float2* target, const dou
   GBC_CUDA(cudaMemcpyAsync(&loss, dl, sizeof(double), cudaMemcpyDeviceToHost, s));
   GBC_CUDA(cudaStreamSynchronize(s));
   cudaFree(dl);
+  check_tc_waits(s);
   return loss;
 }
 
@@ -735,6 +873,7 @@ void cnn_apply_spinor(gbc_ctx* c, Cnn& net, const Spinor& in, const Spinor& out)
   else if (out.prec == PREC_SINGLE) extract_kernel<PrecS><<<g2, 128, 0, c->stream>>>(c->g, V, net.act[net.nlayers], out);
   else extract_kernel<PrecH><<<g2, 128, 0, c->stream>>>(c->g, V, net.act[net.nlayers], out);
   count_launch();
+  check_tc_waits(c->stream);
 }
 
 void cnn_embed_canon(gbc_ctx* c, Cnn& net, int batch, const double* canon_dev, float2* act) {
