@@ -502,7 +502,7 @@ def main():
     # e2e through the public API with pinned host buffers, right after the device-timed steps
     chi_h = torch.from_numpy(src.view(np.float64).copy()).pin_memory()
     psi_h = torch.zeros_like(chi_h).pin_memory()
-    e2e_t, e2e_dev = [], []
+    e2e_t, e2e_dev, e2e_its = [], [], []
     import ctypes as C
     p = G.SolveParams(G.SOLVER_BICGSTAB, G.SYS_FULL, RSD, 10000, DELTA, 10.0, G.PREC_HALF, INNER_TOL, 0, 16, 0, 1)
     # the same K steps as the device-timed loop, each through gbc_solve with pinned host buffers
@@ -515,6 +515,7 @@ def main():
                                C.cast(chi_h.data_ptr(), C.POINTER(C.c_double)), res_arr)
         e2e_t.append(time.perf_counter() - t0)
         e2e_dev.append(res_arr[0].device_seconds)
+        e2e_its.append(max(res_arr[r].n_count for r in range(nsrc)))
         if rc != 0:
             raise RuntimeError("e2e solve failed")
     e2e = max_over_ranks(sum(e2e_t) / len(e2e_t), world) / world
@@ -644,7 +645,8 @@ def main():
         "cpu_baseline": cpu,
         # a zero-guess full-system solve uploads only the sources (gbc_solve skips the psi upload)
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                "device_seconds_median": statistics.median(e2e_dev)},
+                "device_seconds_median": statistics.median(e2e_dev), "steps_seconds": e2e_t,
+                "steps_device_seconds": e2e_dev, "steps_inner_iterations_max": e2e_its},
         "gpu_launches": int(sum(r[0]["launches"] for r in results)),
         "clocks": clk,
         "side_workloads": extras,

@@ -19,6 +19,7 @@
 // the rows into a small matrix, accumulated across blocks with atomics).
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -229,10 +230,10 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], 
 
 // ---- 5th-generation tensor cores (tcgen05) for the forward channel mixing ----------------------
 // One thread issues tcgen05.mma (kind::f16, BF16 in, FP32 accumulate in tensor memory) on
-// shared-memory descriptors of the gathered tile G (128 rows: the block's 96 (site, colour) rows
-// plus zero padding) and the weights W (NU rows = output channels x re/im, padded to a multiple
-// of 16); completion is signalled through an mbarrier by tcgen05.commit, and each warp reads its
-// 32 accumulator lanes back with tcgen05.ld.
+// shared-memory descriptors of the gathered tile G (the MMA's M = 128 rows: the block's 96
+// (site, colour) rows, then 32 rows that overlap the weights and are discarded) and the weights W
+// (NU rows = output channels x re/im, padded to a multiple of 16); completion is signalled through
+// an mbarrier by tcgen05.commit, and each warp reads its 32 accumulator lanes back with tcgen05.ld.
 
 __device__ int g_tc_wait_errors;  // waits for tensor-core completion that gave up (host-checked)
 
@@ -298,12 +299,15 @@ template <int CIN, int COUT>
 __global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, int batch, const float2* links, const float2* hin,
                                                    float2* hout, const __nv_bfloat16* Wr) {
   constexpr int KP = kpad(CIN), NP = npad(COUT), NU = nump(COUT);
-  constexpr int MROWS = 128;  // the MMA's M: the 96 rows of the tile padded with zero rows
+  constexpr int MROWS = 128;  // the MMA's M: the 96 rows of the tile and 32 discarded rows
   static_assert(ROWS <= MROWS && NU <= kTmemCols, "tile does not fit the MMA");
   extern __shared__ __align__(128) unsigned char smem[];
-  __nv_bfloat16* G = reinterpret_cast<__nv_bfloat16*>(smem);  // CoreLayout, MROWS x KP
-  __nv_bfloat16* W = G + MROWS * KP;                          // CoreLayout, NU x KP
-  float2(*lk)[8][9] = reinterpret_cast<float2(*)[8][9]>(W + NU * KP);
+  // G holds the tile's 96 rows; the MMA's rows 96..127 read whatever follows (the weights, the
+  // staged transports or the padding the launch adds): their results are never read back
+  // (likewise the MMA's weight rows NP..NU-1, whose result columns are never read back)
+  __nv_bfloat16* G = reinterpret_cast<__nv_bfloat16*>(smem);  // CoreLayout, ROWS x KP
+  __nv_bfloat16* W = G + ROWS * KP;                           // CoreLayout, NP x KP
+  float2(*lk)[8][9] = reinterpret_cast<float2(*)[8][9]>(W + NP * KP);
   __shared__ int nbr[SITES][9];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
@@ -311,11 +315,7 @@ __global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, int batch, con
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int site0 = blockIdx.x * SITES;
   const CoreLayout<CIN> lay{};
-  for (int p = tid; p < NU * KP; p += blockDim.x) {
-    const int n = p / KP, k = p % KP;
-    W[lay(n, k)] = n < NP ? Wr[(size_t)n * KP + k] : __float2bfloat16(0.f);
-  }
-  for (int p = tid; p < (MROWS - ROWS) * KP; p += blockDim.x) G[ROWS * KP + p] = __float2bfloat16(0.f);
+  for (int p = tid; p < NP * KP; p += blockDim.x) W[lay(p / KP, p % KP)] = Wr[p];
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
                  "r"(kTmemCols));
@@ -541,12 +541,16 @@ void launch_layer(const Geom& g, int V, int batch, const float2* links, const fl
                   const __nv_bfloat16* W, cudaStream_t s) {
   // tile G (128 rows) and weights W (nump rows), bf16 in the tensor cores' core-matrix layout
   // (their bytes are a multiple of 128), then the staged transports (float2)
-  const size_t tile = (size_t)(128 * kpad(CIN) + nump(COUT) * kpad(CIN)) * 2;
+  // G (96 rows) and W (npad rows) in the core-matrix layout, then the staged transports; at least
+  // the 128 rows x kpad that the MMA's A operand (and its B operand, ending earlier) spans
+  const size_t tile = (size_t)(ROWS * kpad(CIN) + npad(COUT) * kpad(CIN)) * 2;
+  const size_t span = (size_t)128 * kpad(CIN) * 2;
   const size_t lkb = sizeof(float2) * SITES * 8 * 9;
-  const size_t smem = batch > 1 ? tile + lkb : tile;
+  const size_t smem = std::max(batch > 1 ? tile + lkb : tile, span);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(layer_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(tile + lkb));
+    cudaFuncSetAttribute(layer_kernel<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)std::max(tile + lkb, span));
     attr = true;
   }
   dim3 grid((V + SITES - 1) / SITES);
