@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--op-only", default=None,
-                    choices=["dslash16", "dslash32", "dslash64", "meo16", "meo64", "meodf", "dslashdf"],
+                    choices=["dslash16", "dslash32", "dslash64", "meo16", "meo64", "meodf", "dslashdf", "precond"],
                     help="profiling mode: set up the workload and time one operator only")
     ap.add_argument("--nrhs", type=int, default=12)
     ap.add_argument("--recon", type=int, default=12, choices=[12, 18])
@@ -75,7 +75,10 @@ def op_only(args):
     ctx = G.Context(dims, 1 / (2 * KAPPA) - 4, CSW, t_boundary=-1, max_rhs=max(12, args.nrhs),
                     sloppy_reconstruct=args.recon)
     ctx.load_gauge(links)
-    op, prec = {"dslash16": (G.OP_DSLASH, G.PREC_HALF), "dslash32": (G.OP_DSLASH, G.PREC_SINGLE),
+    if args.op_only == "precond":
+        ctx.load_precond(WEIGHTS32 if dims == DIMS else WEIGHTS)
+    op, prec = {"precond": (G.TIME_PRECOND, G.PREC_SINGLE),
+                "dslash16": (G.OP_DSLASH, G.PREC_HALF), "dslash32": (G.OP_DSLASH, G.PREC_SINGLE),
                 "dslash64": (G.OP_DSLASH, G.PREC_DOUBLE), "meo16": (G.OP_MEO, G.PREC_HALF),
                 "meo64": (G.OP_MEO, G.PREC_DOUBLE), "meodf": (G.OP_MEO, G.PREC_DF64),
                 "dslashdf": (G.OP_DSLASH, G.PREC_DF64)}[args.op_only]
