@@ -361,7 +361,11 @@ __global__ void __launch_bounds__(CT) layer_kernel(Geom g, int V, int batch, con
                        smem_u32(&mbar))
                    : "memory");
       s_ok = mbar_wait(smem_u32(&mbar), (uint32_t)(b & 1));
-      if (!s_ok) atomicAdd(&g_tc_wait_errors, 1);
+      if (!s_ok) {
+        atomicAdd(&g_tc_wait_errors, 1);
+        // give the MMAs in flight one more bounded wait before their tensor memory is freed
+        (void)mbar_wait(smem_u32(&mbar), (uint32_t)(b & 1));
+      }
     }
     __syncthreads();
     ok = s_ok != 0;
