@@ -164,7 +164,6 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
       int done = 0, iters = 0, outer = 0, reliable = 0, status = GBC_OK;
     };
     std::vector<L> lat(n);
-    const size_t rs_can = 0;
     for (int l = 0; l < n; ++l) {
       gbc_ctx* c = b->ctx[l];
       L& q = lat[l];
@@ -190,7 +189,6 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
       blas_norm2(c->g, q.bd, red(c), s);
       GBC_CUDA(cudaMemcpyAsync(&q.bb, c->d_result, sizeof(double), cudaMemcpyDeviceToHost, s));
     }
-    (void)rs_can;
     GBC_CUDA(cudaStreamSynchronize(s));
     // stencil arguments of the four launches of one CGNE iteration, for every lattice
     std::vector<HopArgs> args(4 * n);
