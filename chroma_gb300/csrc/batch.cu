@@ -205,7 +205,7 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
     GBC_CUDA(cudaMemcpyAsync(b->d_args, args.data(), sizeof(HopArgs) * 4 * n, cudaMemcpyHostToDevice, s));
     const int recon = b->ctx[0]->pf[pidx(sloppy)].recon;
     // GBC_PERSISTENT=1: the inner iterations as one persistent kernel per block of iterations.
-    // The default is one launch per step replayed from CUDA graphs, measured 13-16 % faster on
+    // The default is one launch per step replayed from CUDA graphs, measured 7-13 % faster on
     // GB300 for batches of 33 to 1956 work items (its kernel boundaries cost less than the
     // persistent kernel's 6 software grid barriers per iteration).
     const char* pe = getenv("GBC_PERSISTENT");

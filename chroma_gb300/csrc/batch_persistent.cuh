@@ -8,9 +8,9 @@
 //   te = (..)^dag mp | q = (..)^dag | e += a p, r -= a q, |r|^2 partials | beta (every block) |
 //   p = r + b p |
 // Every block keeps its own copy of every lattice's scalars in shared memory and sums the partials
-// of each lattice in the same fixed order, so all blocks hold bitwise-identical scalars and take
-// identical decisions (skip a converged lattice, stop for a reliable update or when every lattice
-// has converged) without sharing them.
+// of each lattice in the same fixed order (one warp per lattice), so all blocks hold
+// bitwise-identical scalars and take identical decisions (skip a converged lattice, stop for a
+// reliable update or when every lattice has converged) without sharing them.
 //
 // The grid barrier spins on a generation counter with a time limit (about 2 s of SM clock): a wait
 // that runs out sets an error flag, after which every block leaves at its next barrier and the
@@ -72,21 +72,15 @@ __device__ __forceinline__ bool grid_barrier(GridBar* gb, unsigned nblocks, int 
   return ok;
 }
 
-// FP64 sum of n partials, identical in every block (fixed thread mapping and order); every thread
-// gets the total
-__device__ __forceinline__ double block_total(const double* part, int n) {
-  __shared__ double sh[kBatchSites / 32];
+// FP64 sum of n partials by one warp, identical in every block (fixed lane mapping and order);
+// every lane of the warp gets the total.  The lattices of a batch are summed by different warps
+// side by side, so a reduction phase costs one round of loads whatever the number of lattices.
+__device__ __forceinline__ double warp_total(const double* part, int n, int lane) {
   double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += kBatchSites) s += part[i];
+  for (int i = lane; i < n; i += 32) s += part[i];
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
-  __syncthreads();
-  double t = 0.0;
-#pragma unroll
-  for (int q = 0; q < kBatchSites / 32; ++q) t += sh[q];
-  __syncthreads();  // sh is reused by the next call
-  return t;
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  return s;
 }
 
 template <typename PA, typename PO, int RECON, int MINB>
@@ -131,11 +125,11 @@ cg_kernel(const HopArgs* __restrict__ args, const LatCg* __restrict__ lat, const
       if (s_act[wk.x]) hop_body<PO, RECON, HOP_XPAY, false, RED_NORM, kBatchSites, 1>(args[n + wk.x], wk.y, 0);
     }
     if (!(ok = grid_barrier(gb, nb, bar++))) break;
-    // alpha = |r|^2 / |M~ p|^2 per lattice
-    for (int l = 0; l < n; ++l) {
+    // alpha = |r|^2 / |M~ p|^2 per lattice (warp w sums lattices w, w + 4, ...)
+    for (int l = tid >> 5; l < n; l += kBatchSites / 32) {
       if (!s_act[l]) continue;
-      const double d = block_total(lat[l].hop_part, lat[l].nblk);
-      if (tid == 0) {
+      const double d = warp_total(lat[l].hop_part, lat[l].nblk, tid & 31);
+      if ((tid & 31) == 0) {
         s_d[l] = d;
         s_a[l] = d > 0.0 ? s_c[l] / d : 0.0;
       }
@@ -158,11 +152,11 @@ cg_kernel(const HopArgs* __restrict__ args, const LatCg* __restrict__ lat, const
       if (s_act[wk.x]) batch_update_block<PA, PO>(lat[wk.x], wk.y, s_a[wk.x]);
     }
     if (!(ok = grid_barrier(gb, nb, bar++))) break;
-    // beta, convergence and the reliable-update trigger per lattice
-    for (int l = 0; l < n; ++l) {
+    // beta, convergence and the reliable-update trigger per lattice (warp w: lattices w, w + 4, ...)
+    for (int l = tid >> 5; l < n; l += kBatchSites / 32) {
       if (!s_act[l]) continue;
-      const double cp = block_total(lat[l].upd_part, lat[l].nblk);
-      if (tid == 0) {
+      const double cp = warp_total(lat[l].upd_part, lat[l].nblk, tid & 31);
+      if ((tid & 31) == 0) {
         const double c = s_c[l];
         const int act = cp > s_rsd[l];
         s_cp[l] = cp;
@@ -181,6 +175,7 @@ cg_kernel(const HopArgs* __restrict__ args, const LatCg* __restrict__ lat, const
         }
       }
     }
+    __syncthreads();  // every lattice's scalars updated
     if (tid == 0) {
       int any = 0;
       for (int l = 0; l < n; ++l) any |= s_act[l];
