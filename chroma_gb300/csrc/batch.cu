@@ -205,9 +205,9 @@ int gbc_batch_solve(gbc_batch* b, const gbc_solve_params* pp, double* const* psi
     GBC_CUDA(cudaMemcpyAsync(b->d_args, args.data(), sizeof(HopArgs) * 4 * n, cudaMemcpyHostToDevice, s));
     const int recon = b->ctx[0]->pf[pidx(sloppy)].recon;
     // GBC_PERSISTENT=1: the inner iterations as one persistent kernel per block of iterations.
-    // The default is one launch per step replayed from CUDA graphs, measured 7-13 % faster on
-    // GB300 for batches of 33 to 1956 work items (its kernel boundaries cost less than the
-    // persistent kernel's 6 software grid barriers per iteration).
+    // The default is one launch per step replayed from CUDA graphs: on GB300 it matches the
+    // persistent kernel on a batch of 33 work items and is 10 % faster on one of 1956 (its kernel
+    // boundaries cost less than the persistent kernel's 5 software grid barriers per iteration).
     const char* pe = getenv("GBC_PERSISTENT");
     bool persist = pe && pe[0] == '1' && n <= kPersistMaxLattices && pa == S && sloppy != D;
     auto multi = [&](int k, int mode, bool dag, bool reduce) {

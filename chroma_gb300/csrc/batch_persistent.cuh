@@ -3,10 +3,10 @@
 // lattice), walking the batch's work table of (lattice, 128-site block) pairs with a grid-stride
 // loop, so the GPU stays busy across lattices of different sizes without a launch per step.
 //
-// Per iteration, 6 grid barriers separate the passes that read another block's output:
+// Per iteration, 5 grid barriers separate the passes that read another block's output:
 //   te = A_ee^-1 D_eo p | mp = A_oo p - 1/4 D_oe te, |mp|^2 partials | alpha (every block) |
-//   te = (..)^dag mp | q = (..)^dag | e += a p, r -= a q, |r|^2 partials | beta (every block) |
-//   p = r + b p |
+//   te = (..)^dag mp | q = (..)^dag mp in registers, e += a p, r -= a q, |r|^2 partials |
+//   beta (every block) | p = r + b p |
 // Every block keeps its own copy of every lattice's scalars in shared memory and sums the partials
 // of each lattice in the same fixed order (one warp per lattice), so all blocks hold
 // bitwise-identical scalars and take identical decisions (skip a converged lattice, stop for a
@@ -83,6 +83,58 @@ __device__ __forceinline__ double warp_total(const double* part, int n, int lane
   return s;
 }
 
+// q = M~^dag mp at the block's odd sites (the isign-MINUS XPAY epilogue of a, kept in registers)
+// fused with the CG update e += alpha p, r -= alpha q, and |r|^2 of the block -> l.upd_part
+template <typename PA, typename PO, int RECON>
+__device__ __forceinline__ void xpay_dag_update_block(const HopArgs& a, const LatCg& l, int sblock, double alpha) {
+  static_assert(std::is_same<typename PO::real, float>::value && std::is_same<typename PA::real, float>::value,
+                "FP32-arithmetic stencil and accumulators");
+  const int idx = sblock * kBatchSites + threadIdx.x;
+  float accr = 0.f;
+  if (idx < a.g.Vh) {
+    const Coord c = cb_coords(a.g, idx, a.out_parity);
+    const char* in = (const char*)a.in;
+    float2 accf[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) accf[k] = make_float2(0.f, 0.f);
+    hop_dir_f2<PO, RECON, 0, true>(accf, a, c, idx, in, a.in_norm);
+    hop_dir_f2<PO, RECON, 1, true>(accf, a, c, idx, in, a.in_norm);
+    hop_dir_f2<PO, RECON, 2, true>(accf, a, c, idx, in, a.in_norm);
+    hop_dir_f2<PO, RECON, 3, true>(accf, a, c, idx, in, a.in_norm);
+    cplx<float> acc[12], q[12], self[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) acc[k] = {accf[k].x, accf[k].y};
+    hop_epilogue_value<PO, HOP_XPAY, true>(a, 0, idx, acc, q, self);
+    cplx<float> es[12], rs[12], ps[12];
+    ldf<PA>(es, l.e, idx);
+    ldf<PA>(rs, l.r, idx);
+    ldf<PO>(ps, l.p, idx);
+    const float al = (float)alpha;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      es[k].re = fmadd(al, ps[k].re, es[k].re);
+      es[k].im = fmadd(al, ps[k].im, es[k].im);
+      rs[k].re = fmadd(-al, q[k].re, rs[k].re);
+      rs[k].im = fmadd(-al, q[k].im, rs[k].im);
+      accr = fmadd(rs[k].re, rs[k].re, fmadd(rs[k].im, rs[k].im, accr));
+    }
+    stf<PA>(l.e, idx, es);
+    stf<PA>(l.r, idx, rs);
+  }
+  __shared__ double sh[kBatchSites / 32];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) accr += __shfl_down_sync(0xffffffffu, accr, off);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)accr;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+#pragma unroll
+    for (int q = 0; q < kBatchSites / 32; ++q) t += sh[q];
+    l.upd_part[sblock] = t;
+  }
+  __syncthreads();  // sh is reused by the next call
+}
+
 template <typename PA, typename PO, int RECON, int MINB>
 __global__ void __launch_bounds__(kBatchSites, MINB)
 cg_kernel(const HopArgs* __restrict__ args, const LatCg* __restrict__ lat, const int2* __restrict__ work, int nwork,
@@ -141,15 +193,10 @@ cg_kernel(const HopArgs* __restrict__ args, const LatCg* __restrict__ lat, const
       if (s_act[wk.x]) hop_body<PO, RECON, HOP_CLOV, true, RED_NONE, kBatchSites, 1>(args[2 * n + wk.x], wk.y, 0);
     }
     if (!(ok = grid_barrier(gb, nb, bar++))) break;
+    // with q = M~^dag mp in registers: e += a p ; r -= a q with |r|^2 per block
     for (int w = blockIdx.x; w < nwork; w += nb) {
       const int2 wk = work[w];
-      if (s_act[wk.x]) hop_body<PO, RECON, HOP_XPAY, true, RED_NONE, kBatchSites, 1>(args[3 * n + wk.x], wk.y, 0);
-    }
-    if (!(ok = grid_barrier(gb, nb, bar++))) break;
-    // e += a p ; r -= a q with |r|^2 per block
-    for (int w = blockIdx.x; w < nwork; w += nb) {
-      const int2 wk = work[w];
-      if (s_act[wk.x]) batch_update_block<PA, PO>(lat[wk.x], wk.y, s_a[wk.x]);
+      if (s_act[wk.x]) xpay_dag_update_block<PA, PO, RECON>(args[3 * n + wk.x], lat[wk.x], wk.y, s_a[wk.x]);
     }
     if (!(ok = grid_barrier(gb, nb, bar++))) break;
     // beta, convergence and the reliable-update trigger per lattice (warp w: lattices w, w + 4, ...)

@@ -544,6 +544,12 @@ __device__ __forceinline__ Sums3<typename P::real> store_site(const HopArgs& a, 
   return site;
 }
 
+template <typename P, int MODE, bool DAG>
+__device__ __forceinline__ void hop_epilogue_value(const HopArgs& a, int rhs, int idx,
+                                                   const cplx<typename P::real> (&acc)[12],
+                                                   cplx<typename P::real> (&out)[12],
+                                                   cplx<typename P::real> (&self)[12]);
+
 // The MODE epilogue of one output site: out = a D' psi, T (a D' psi) or T self + a D' psi
 // (+ twist), stored in the output precision; returns the site sums of the REDUCE kind.
 template <typename P, int MODE, bool DAG, int REDUCE>
@@ -551,10 +557,21 @@ __device__ __forceinline__ Sums3<typename P::real> hop_epilogue(const HopArgs& a
                                                                 const cplx<typename P::real> (&acc)[12]) {
   static_assert(REDUCE != RED_DOT_SELF || MODE == HOP_XPAY, "(out, self) needs the XPAY epilogue");
   using T = typename P::real;
-  const Geom& g = a.g;
-  const T coef = (T)a.a;
   cplx<T> out[12];
   cplx<T> self[12];
+  hop_epilogue_value<P, MODE, DAG>(a, rhs, idx, acc, out, self);
+  return store_site<P, REDUCE>(a, rhs, idx, out, self);
+}
+
+// The output value of the MODE epilogue at one site (self: the XPAY operand, loaded here)
+template <typename P, int MODE, bool DAG>
+__device__ __forceinline__ void hop_epilogue_value(const HopArgs& a, int rhs, int idx,
+                                                   const cplx<typename P::real> (&acc)[12],
+                                                   cplx<typename P::real> (&out)[12],
+                                                   cplx<typename P::real> (&self)[12]) {
+  using T = typename P::real;
+  const Geom& g = a.g;
+  const T coef = (T)a.a;
   if constexpr (MODE == HOP_PLAIN) {
 #pragma unroll
     for (int k = 0; k < 12; ++k) out[k] = coef * acc[k];
@@ -599,7 +616,6 @@ __device__ __forceinline__ Sums3<typename P::real> hop_epilogue(const HopArgs& a
       }
     }
   }
-  return store_site<P, REDUCE>(a, rhs, idx, out, self);
 }
 
 template <typename P, int RECON, int MODE, bool DAG, int REDUCE, int TX, int NRB, int MINB>

@@ -237,11 +237,12 @@ struct PersistLat {
 constexpr int kPersistMaxLattices = 32;
 // Runs up to kmax CGNE iterations of every active lattice in one cooperative launch (grid = the
 // co-resident blocks, at most nwork): the four stencil passes, the update and p = r + b p walk the
-// work table, alpha and beta are summed by every block from the partials (identical sums in every
-// block, so no scalar is shared), 6 grid barriers per iteration.  Stops when no lattice is active,
-// or after an iteration (every fourth of the launch) in which an active lattice's |r| fell below
-// delta * maxrr or rose above at_update (a reliable update is due); writes the CGScalars and PersistLat back and
-// out[0] = iterations run.  Returns 0, -1 when (pa, po, recon) has no persistent variant or the
+// work table (the update fused into the second M~^dag pass), alpha and beta are summed by every
+// block from the partials (identical sums in every block, so no scalar is shared), 5 grid
+// barriers per iteration.  Stops when no lattice is active, or after an iteration (every fourth of
+// the launch) in which an active lattice's |r| fell below delta * maxrr or rose above at_update (a
+// reliable update is due); writes the CGScalars and PersistLat back and out[0] = iterations run.
+// Returns 0, -1 when (pa, po, recon) has no persistent variant or the
 // cooperative launch is refused (the caller then uses the per-launch path), or the CUDA error.
 int batch_cg_persistent(int pa, int po, int recon, const HopArgs* args, const LatCg* lat, const int2* work,
                         int nwork, int n, int kmax, double delta, PersistLat* pl, GridBar* bar, int* out,
