@@ -319,8 +319,15 @@ void iteration(gbc_ctx* c, int po, BiScal* sc, int n, const Spinor& x, const Spi
                const Spinor& p, const Spinor& v, const Spinor& s, const Spinor& t, const Spinor& te) {
   cudaStream_t st = c->stream;
   const int nth = ((n + 31) / 32) * 32;  // one thread per right-hand side
-  apply_meo(c, po, false, p, v, te, RED_NONE);
-  blas_cdot(c->g, r0, v, red(c), st);
+  if (!c->sym && r0.prec == PREC_SINGLE) {
+    // (r0, v) summed in the epilogue of the stencil launch that writes v = M~ p (r0 at its sites)
+    c->hop_aux = r0;
+    apply_meo(c, po, false, p, v, te, RED_DOT_AUX);
+    c->hop_aux = Spinor{};
+  } else {
+    apply_meo(c, po, false, p, v, te, RED_NONE);
+    blas_cdot(c->g, r0, v, red(c), st);
+  }
   bi_alpha<<<1, nth, 0, st>>>(sc, c->d_result, n);
   count_launch();
   run<0>(c, n, sc, SUpdF<PA, PO>{sc, r, v, s});

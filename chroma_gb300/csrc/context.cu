@@ -275,7 +275,7 @@ static int default_shape(int prec, int nrhs) {
 int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, int reduce, const HopArgs& h) {
   // (precision, epilogue, isign, reduction) in the high bits, nrhs (any size) in the low 32
   const long long key =
-      ((((long long)pidx(prec) * 4 + mode) * 2 + (dag ? 1 : 0)) * 3 + reduce) << 32 | (unsigned)h.nrhs;
+      ((((long long)pidx(prec) * 4 + mode) * 2 + (dag ? 1 : 0)) * 4 + reduce) << 32 | (unsigned)h.nrhs;
   auto it = c->tuned.find(key);
   if (it != c->tuned.end()) return it->second;
   int best = default_shape(prec, h.nrhs);
@@ -411,13 +411,18 @@ void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, con
   h.part_stride = c->part_stride;
   h.active = c->hop_active;
   h.active_stride = c->hop_active_stride;
+  if (reduce == RED_DOT_AUX) {
+    if (!c->hop_aux.v || c->hop_aux.prec != PREC_SINGLE) throw std::string("(aux, out) reduction without an FP32 aux field");
+    h.aux = c->hop_aux.v;
+    h.aux_rhs_bytes = c->hop_aux.rhs_bytes;
+  }
   const HopShape sh = kHopShapes[tuned_shape(c, prec, f.recon, mode, dag, reduce, h)];
   if (hop_blocks(sh, h.g.Vh) > c->part_stride) throw std::string("partials buffer too small");
   int nb = hop_launch(prec, f.recon, mode, dag, reduce, h, sh, c->stream);
   if (nb < 0) throw std::string("hopping kernel variant not compiled");
   count_launch();
   GBC_CUDA(cudaGetLastError());
-  if (reduce) reduce_finalize(red(c), reduce == RED_DOT_SELF ? 3 : 1, in.nrhs, nb, c->stream);
+  if (reduce) reduce_finalize(red(c), red_rows(reduce), in.nrhs, nb, c->stream);
 }
 
 void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& out, const Spinor& tmp_e, int reduce) {

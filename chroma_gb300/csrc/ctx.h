@@ -110,6 +110,7 @@ struct gbc_ctx {
   // inner BiCGStab points them at its scalars so that converged right-hand sides cost nothing
   const int* hop_active = nullptr;
   int hop_active_stride = 0;
+  gbc::Spinor hop_aux{};  // the FP32 field of a RED_DOT_AUX stencil launch (set around the call)
   // second stream for the host copies of gbc_solve that overlap device work (created on first use)
   cudaStream_t copy_stream = nullptr;
 };

@@ -498,14 +498,14 @@ template <typename P, int RECON, int MODE, bool DAG, int REDUCE, int TX, int NRB
 __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group);
 
 // site sums of a fused reduction (RED_NORM: q[0] = |out|^2; RED_DOT_SELF: q = Re, Im (out, self),
-// |out|^2), in the compute precision
+// |out|^2; RED_DOT_AUX: q = Re, Im (aux, out)), in the compute precision
 template <typename T>
 struct Sums3 {
   T q[3];
 };
 template <int RED>
 __host__ __device__ constexpr int red_count() {
-  return RED == RED_DOT_SELF ? 3 : RED == RED_NORM ? 1 : 0;
+  return RED == RED_DOT_SELF ? 3 : RED == RED_DOT_AUX ? 2 : RED == RED_NORM ? 1 : 0;
 }
 template <typename T>
 __device__ __forceinline__ Sums3<T> operator+(Sums3<T> a, const Sums3<T>& b) {
@@ -531,6 +531,19 @@ __device__ __forceinline__ Sums3<typename P::real> store_site(const HopArgs& a, 
     for (int k = 0; k < 12; ++k) nn = fmadd(out[k].re, out[k].re, fmadd(out[k].im, out[k].im, nn));
     site.q[REDUCE == RED_DOT_SELF ? 2 : 0] = nn;
   }
+  if constexpr (REDUCE == RED_DOT_AUX) {
+    // (aux, out) = sum conj(aux) out, aux an FP32 field at the output site
+    cplx<float> x[12];
+    load_spinor<PrecS>(x, (const char*)a.aux + (size_t)rhs * a.aux_rhs_bytes, nullptr, idx, a.g.stride);
+    T re = 0, im = 0;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      re = fmadd((T)x[k].re, out[k].re, fmadd((T)x[k].im, out[k].im, re));
+      im = fmadd((T)x[k].re, out[k].im, fmadd(-(T)x[k].im, out[k].re, im));
+    }
+    site.q[0] = re;
+    site.q[1] = im;
+  }
   if constexpr (REDUCE == RED_DOT_SELF) {
     T re = 0, im = 0;
 #pragma unroll
@@ -555,7 +568,8 @@ __device__ __forceinline__ void hop_epilogue_value(const HopArgs& a, int rhs, in
 template <typename P, int MODE, bool DAG, int REDUCE>
 __device__ __forceinline__ Sums3<typename P::real> hop_epilogue(const HopArgs& a, int rhs, int idx,
                                                                 const cplx<typename P::real> (&acc)[12]) {
-  static_assert(REDUCE != RED_DOT_SELF || MODE == HOP_XPAY, "(out, self) needs the XPAY epilogue");
+  static_assert((REDUCE != RED_DOT_SELF && REDUCE != RED_DOT_AUX) || MODE == HOP_XPAY,
+                "the dot-product reductions are fused into the XPAY epilogue");
   using T = typename P::real;
   cplx<T> out[12];
   cplx<T> self[12];

@@ -111,6 +111,10 @@ static int hop_mode_reduce(int mode, int reduce, const HopArgs& a, HopShape sh, 
         if constexpr (!DAG) return hop_shape<P, RECON, HOP_XPAY, DAG, RED_DOT_SELF>(a, sh, s);
         return -1;
       }
+      if (reduce == RED_DOT_AUX) {
+        if constexpr (!DAG) return hop_shape<P, RECON, HOP_XPAY, DAG, RED_DOT_AUX>(a, sh, s);
+        return -1;
+      }
       return hop_shape<P, RECON, HOP_XPAY, DAG, RED_NONE>(a, sh, s);
   }
   return -1;
@@ -132,7 +136,7 @@ static int hop_multi_mode(int mode, int reduce, const HopArgs* args, const int2*
     case HOP_PLAIN: hop_kernel_multi<P, RECON, HOP_PLAIN, DAG, RED_NONE><<<nwork, 128, 0, s>>>(args, work); return nwork;
     case HOP_CLOV: hop_kernel_multi<P, RECON, HOP_CLOV, DAG, RED_NONE><<<nwork, 128, 0, s>>>(args, work); return nwork;
     case HOP_XPAY:
-      if (reduce == RED_DOT_SELF) return -1;
+      if (reduce == RED_DOT_SELF || reduce == RED_DOT_AUX) return -1;
       if (reduce) hop_kernel_multi<P, RECON, HOP_XPAY, DAG, RED_NORM><<<nwork, 128, 0, s>>>(args, work);
       else hop_kernel_multi<P, RECON, HOP_XPAY, DAG, RED_NONE><<<nwork, 128, 0, s>>>(args, work);
       return nwork;

@@ -12,8 +12,10 @@ long long launch_count();
 
 enum { HOP_PLAIN = 0, HOP_CLOV = 1, HOP_XPAY = 2 };
 // reductions fused into the stencil epilogue: none; |out|^2; (out, self) and |out|^2 of the XPAY
-// epilogue (BiCGStab's (t, s), (t, t) for t = M~ s), three partial rows per right-hand side
-enum { RED_NONE = 0, RED_NORM = 1, RED_DOT_SELF = 2 };
+// epilogue (BiCGStab's (t, s), (t, t) for t = M~ s), three partial rows per right-hand side;
+// (aux, out) of the XPAY epilogue with aux an FP32 field (BiCGStab's (r0, v) for v = M~ p), two rows
+enum { RED_NONE = 0, RED_NORM = 1, RED_DOT_SELF = 2, RED_DOT_AUX = 3 };
+inline int red_rows(int reduce) { return reduce == RED_DOT_SELF ? 3 : reduce == RED_DOT_AUX ? 2 : reduce ? 1 : 0; }
 enum { PREC_HALF = 2, PREC_SINGLE = 4, PREC_DOUBLE = 8 };
 // internal arithmetic mode, not a storage precision: FP64-stored fields, double-float arithmetic
 // (the PrecDF kernels on the split copies of the FP64 links and clover)
@@ -63,6 +65,9 @@ struct HopArgs {
   // flag is 0 is skipped (no loads, no store, zero partials); nullptr = all active
   const int* active;
   int active_stride;
+  // RED_DOT_AUX: the FP32 field (per right-hand side, planes of stride g.stride) dotted with out
+  const void* aux;
+  size_t aux_rhs_bytes;
 };
 
 // Launch geometry chosen by the caller (autotuned): TX sites x NRB right-hand sides per block,
