@@ -509,6 +509,8 @@ def main():
     import ctypes as C
     p = G.SolveParams(G.SOLVER_BICGSTAB, G.SYS_FULL, RSD, 10000, DELTA, 10.0, G.PREC_HALF, INNER_TOL, 0, 16, 0, 1)
     # the same K steps as the device-timed loop, each through gbc_solve with pinned host buffers
+    e2e_clocks = Clocks()
+    e2e_clocks.start()
     for i in range(args.steps):
         flush.random_()
         torch.cuda.synchronize()
@@ -521,6 +523,7 @@ def main():
         e2e_its.append(max(res_arr[r].n_count for r in range(nsrc)))
         if rc != 0:
             raise RuntimeError("e2e solve failed")
+    e2e_clk = e2e_clocks.stop()
     e2e = max_over_ranks(sum(e2e_t) / len(e2e_t), world) / world
     nbytes = src.nbytes
 
@@ -649,7 +652,7 @@ def main():
         # a zero-guess full-system solve uploads only the sources (gbc_solve skips the psi upload)
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                 "device_seconds_median": statistics.median(e2e_dev), "steps_seconds": e2e_t,
-                "steps_device_seconds": e2e_dev, "steps_inner_iterations_max": e2e_its},
+                "steps_device_seconds": e2e_dev, "steps_inner_iterations_max": e2e_its, "clocks": e2e_clk},
         "gpu_launches": int(sum(r[0]["launches"] for r in results)),
         "clocks": clk,
         "side_workloads": extras,

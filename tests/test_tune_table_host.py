@@ -45,7 +45,7 @@ def test_entries_match_the_compiled_shapes():
     table = entries()
     assert table
     pat = re.compile(r"^[^|]+\|cc\d+\|\d+x\d+x\d+x\d+\|prec=(2|4|8|16)\|recon=(12|18)\|mode=[012]\|dag=[01]\|"
-                     r"reduce=[012]\|nrhs=\d+\|shapes=([0-9a-f]{8})$")
+                     r"reduce=[0123]\|nrhs=\d+\|shapes=([0-9a-f]{8})$")
     for key, shape in table.items():
         m = pat.match(key)
         assert m, key
@@ -60,3 +60,6 @@ def test_table_covers_the_propagator_solve():
     for want in [("2", "1", "12"), ("2", "2", "12"), ("16", "1", "12"), ("16", "2", "12"), ("16", "0", "12"),
                  ("8", "0", "12"), ("8", "2", "12")]:
         assert want in have, want
+    # the BiCGStab launches with fused reductions: (t, s), (t, t) and (r0, v)
+    assert any("|32x32x32x64|prec=2|" in k and "|reduce=2|nrhs=12|" in k for k in lat)
+    assert any("|32x32x32x64|prec=2|" in k and "|reduce=3|nrhs=12|" in k for k in lat)
