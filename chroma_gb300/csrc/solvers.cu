@@ -38,7 +38,7 @@ namespace {
 enum {
   SLOT_X = 1, SLOT_B, SLOT_R, SLOT_P, SLOT_MP, SLOT_MMP, SLOT_TE, SLOT_T1, SLOT_T2, SLOT_TEH,
   SLOT_XD, SLOT_BD, SLOT_RD, SLOT_TD1, SLOT_TD2, SLOT_TED, SLOT_ES, SLOT_RS, SLOT_CHIE, SLOT_PSIE, SLOT_SE,
-  SLOT_XS, SLOT_RHS
+  SLOT_XS, SLOT_RHS, SLOT_CHIO
 };
 
 struct Batch {
@@ -789,6 +789,14 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   const char* odf = getenv("GBC_OUTER_DF");
   const int DX = (odf && odf[0] == '0') || symmetric || p.system != GBC_SYS_FULL ? D : PREC_DF;
   if (DX == PREC_DF) ensure_prec(c, PREC_DF);
+  // In the defect correction the Schur-prepared source chi'_o only seeds the first inner solve,
+  // whose tolerance is far coarser than FP32 rounding, so it is formed with the FP32 operator;
+  // every outer residual then comes from the original source instead of chi'_o,
+  //   r = chi_o - A_oo psi + 1/2 D_oe A_ee^-1 (chi_e + 1/2 D_eo psi)   (= chi'_o - M~ psi),
+  // in double-float arithmetic: one stencil launch fewer in that arithmetic per solve.
+  const bool approx_prep = DX == PREC_DF && !c->act.twisted && sloppy != PREC_DOUBLE &&
+                           (p.solver == GBC_SOLVER_MIXED || p.solver == GBC_SOLVER_FGMRES ||
+                            p.solver == GBC_SOLVER_BICGSTAB);
   if (symmetric) {
     // A_oo^-1 packed before any iteration is captured into a graph
     ensure_sym(c, D);
@@ -811,16 +819,28 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
   const PrecFields& fd = c->pf[pidx(D)];
 
   import_spinor(g, chi_canon, rs, 1, chi, s);
-  Spinor chie, psie;
+  Spinor chie, psie, chio;
   if (p.system == GBC_SYS_FULL) {
     // Schur prep (eoprec_fermact_qprop.cc:47-54): chi'_o = chi_o - (-1/2 D_oe) A_ee^-1 chi_e
     chie = sub(workspace(c, SLOT_CHIE, D, n), 0, n);
     psie = sub(workspace(c, SLOT_PSIE, D, n), 0, n);
     import_spinor(g, chi_canon, rs, 0, chie, s);
     std::vector<double> no = norm2(c, chi), ne = norm2(c, chie);
-    apply_clover(c, DX, 0, true, chie, ted);
-    hop(c, DX, 1, HOP_PLAIN, false, 0.5, ted, t1, nullptr, nullptr, false);
-    blas_xpy(g, chi, t1, s);
+    if (approx_prep) {
+      chio = sub(workspace(c, SLOT_CHIO, D, n), 0, n);
+      blas_copy(g, chio, chi, s);
+      // the FP32 fields of the inner solver's workspaces (the same slots and precision below)
+      Spinor ae = sub(workspace(c, SLOT_ES, PREC_SINGLE, n), 0, n);
+      Spinor at = sub(workspace(c, SLOT_RS, PREC_SINGLE, n), 0, n);
+      blas_copy(g, ae, chie, s);
+      apply_clover(c, PREC_SINGLE, 0, true, ae, at);
+      hop(c, PREC_SINGLE, 1, HOP_PLAIN, false, 0.5, at, ae, nullptr, nullptr, false);
+      blas_xpy(g, chi, ae, s);
+    } else {
+      apply_clover(c, DX, 0, true, chie, ted);
+      hop(c, DX, 1, HOP_PLAIN, false, 0.5, ted, t1, nullptr, nullptr, false);
+      blas_xpy(g, chi, t1, s);
+    }
     // the even reconstruction is exact, so the full residual equals the odd one: solve the odd
     // system to target * |chi| / |chi'_o| so that |M psi - chi| / |chi| meets the target
     std::vector<double> np = norm2(c, chi);
@@ -937,6 +957,15 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
         GBC_CUDA(cudaMemcpyAsync(c->d_cb, c->h_coef + n, sizeof(double2) * n, cudaMemcpyHostToDevice, s));
         blas_axpby(g, c->d_ca, ta, c->d_cb, rd, s);
         blas_norm2(g, rd, red(c), s);
+        rr_exact = false;
+      } else if (approx_prep) {
+        // r = chi_o - (A_oo psi - 1/2 D_oe A_ee^-1 (chi_e + 1/2 D_eo psi)) from the original
+        // source, in double-float arithmetic on the FP64 fields
+        hop(c, DX, 0, HOP_PLAIN, false, 0.5, psi, ted, nullptr, nullptr, false);
+        blas_xpy(g, ted, chie, s);
+        apply_clover(c, DX, 0, true, ted, t2);
+        hop(c, DX, 1, HOP_XPAY, false, -0.5, t2, rd, &psi, c->pf[pidx(DX)].clov[1], false);
+        blas_xmy_norm2(g, chio, rd, red(c), s);
         rr_exact = false;
       } else {
         // residual with the FP64 fields (double-float arithmetic unless GBC_OUTER_DF=0)
