@@ -381,9 +381,28 @@ int tuned_shape(gbc_ctx* c, int prec, int recon, int mode, bool dag, int reduce,
   return best;
 }
 
-void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, const Spinor& in, const Spinor& out,
-         const Spinor* self, const void* clov, int reduce, double twist) {
+// The (hi, lo) float copy of an FP64 field that the double-float kernels read (same bytes and
+// index as the field), in workspace slot `slot`.
+static Spinor split_copy(gbc_ctx* c, int slot, const Spinor& x) {
+  if (x.prec != PREC_DOUBLE) throw std::string("double-float operands are FP64 fields");
+  Spinor t = sub(workspace(c, slot, PREC_DOUBLE, x.nrhs), 0, x.nrhs);
+  if (t.rhs_bytes != x.rhs_bytes) throw std::string("double-float operand with a foreign layout");
+  split_df64((const double*)x.v, (float2*)t.v, (size_t)x.nrhs * x.rhs_bytes / sizeof(double), c->stream);
+  GBC_CUDA(cudaGetLastError());
+  return t;
+}
+
+void hop(gbc_ctx* c, int prec, int out_parity, int mode, bool dag, double a, const Spinor& in_field,
+         const Spinor& out, const Spinor* self, const void* clov, int reduce, double twist) {
   const PrecFields& f = c->pf[pidx(prec)];
+  Spinor in = in_field, self_split;
+  if (prec == PREC_DF) {
+    in = split_copy(c, 960, in_field);
+    if (self) {
+      self_split = split_copy(c, 961, *self);
+      self = &self_split;
+    }
+  }
   HopArgs h{};
   h.g = c->g;
   h.out_parity = out_parity;
@@ -436,8 +455,8 @@ void apply_meo(gbc_ctx* c, int prec, bool dag, const Spinor& in, const Spinor& o
 void apply_clover(gbc_ctx* c, int prec, int parity, bool inverse, const Spinor& in, const Spinor& out) {
   if (inverse && parity == 1) ensure_sym(c, prec);
   const PrecFields& f = c->pf[pidx(prec)];
-  blas_clover(c->g, inverse ? (parity == 0 ? f.clovinv : f.clovinv_odd) : f.clov[parity], out, in, c->stream,
-              prec == PREC_DF);
+  blas_clover(c->g, inverse ? (parity == 0 ? f.clovinv : f.clovinv_odd) : f.clov[parity], out,
+              prec == PREC_DF ? split_copy(c, 962, in) : in, c->stream, prec == PREC_DF);
   GBC_CUDA(cudaGetLastError());
 }
 

@@ -287,14 +287,18 @@ __device__ __forceinline__ void load_spinor<PrecH>(cplx<float> (&s)[12], const v
   }
 }
 
+// A double-float kernel reads its spinor operands from their split copies (made once per launch by
+// split_df64: every double2 (re, im) of the FP64 field as a float4 (re.hi, re.lo, im.hi, im.lo),
+// same bytes and index), so a neighbour spinor costs no conversion at each of its 8 uses; results
+// are stored as FP64.
 template <>
 __device__ __forceinline__ void load_spinor<PrecDF>(cplx<df64> (&s)[12], const void* base, const float*, int idx,
                                                     int stride) {
-  const double2* p = reinterpret_cast<const double2*>(base);
+  const float4* p = reinterpret_cast<const float4*>(base);
 #pragma unroll
   for (int k = 0; k < 12; ++k) {
-    double2 v = ldw(p + (size_t)k * stride + idx);
-    s[k] = {df64_from_bits(v.x), df64_from_bits(v.y)};
+    float4 v = ldw(p + (size_t)k * stride + idx);
+    s[k] = {df64(v.x, v.y), df64(v.z, v.w)};
   }
 }
 
