@@ -292,6 +292,28 @@ struct XpyF {
   }
 };
 
+// x -= y (y may be lower precision);  acc = |x|^2
+template <typename PX, typename PY>
+struct XsubNormF {
+  using Acc = typename PX::real;
+  Spinor x, y;
+  __device__ void operator()(int idx, int r, Acc* acc) const {
+    using T = typename PX::real;
+    cplx<T> xs[12];
+    cplx<typename PY::real> ys[12];
+    ld<PX>(xs, x, idx, r);
+    ld<PY>(ys, y, idx, r);
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      xs[k] = xs[k] - cplx<T>{(T)ys[k].re, (T)ys[k].im};
+      s = fmadd(xs[k].re, xs[k].re, fmadd(xs[k].im, xs[k].im, s));
+    }
+    st<PX>(x, idx, r, xs);
+    acc[0] += s;
+  }
+};
+
 __global__ void finalize_kernel(const double* partials, int part_stride, int nblocks, double* result) {
   // one block per (quantity, rhs); fixed-order tree => bitwise repeatable
   const int qr = blockIdx.x;
@@ -418,6 +440,9 @@ void blas_shift_axpy(const Geom& g, const double* sigma, const Spinor& x, const 
 }
 void blas_xpy(const Geom& g, const Spinor& x, const Spinor& y, cudaStream_t s) {
   GBC_DISPATCH2(x.prec, y.prec, (run<0>(g, x.nrhs, XpyF<PA, PB>{x, y}, nullptr, s)));
+}
+void blas_xsub_norm2(const Geom& g, const Spinor& x, const Spinor& y, const Red& red, cudaStream_t s) {
+  GBC_DISPATCH2(x.prec, y.prec, (run<1>(g, x.nrhs, XsubNormF<PA, PB>{x, y}, &red, s)));
 }
 
 void cg_alpha(CGScalars* st, const double* red_d, double* a_out, int nrhs, cudaStream_t s) {

@@ -196,6 +196,8 @@ void blas_shift_dot(const Geom& g, const double* sigma, const Spinor& x, const S
 void blas_shift_axpy(const Geom& g, const double* sigma, const Spinor& x, const Spinor& y, cudaStream_t s);
 // x += y (y may be lower precision)
 void blas_xpy(const Geom& g, const Spinor& x, const Spinor& y, cudaStream_t s);
+// x -= y (y may be lower precision), result = |x|^2
+void blas_xsub_norm2(const Geom& g, const Spinor& x, const Spinor& y, const Red& red, cudaStream_t s);
 // finalize the partial sums of nred quantities x nrhs into red.result
 void reduce_finalize(const Red& red, int nred, int nrhs, int nblocks, cudaStream_t s);
 

@@ -820,12 +820,14 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
 
   import_spinor(g, chi_canon, rs, 1, chi, s);
   Spinor chie, psie, chio;
+  std::vector<double> src_no, src_ne, src_np;  // |chi_o|^2, |chi_e|^2, |chi'_o|^2 of the full system
   if (p.system == GBC_SYS_FULL) {
     // Schur prep (eoprec_fermact_qprop.cc:47-54): chi'_o = chi_o - (-1/2 D_oe) A_ee^-1 chi_e
     chie = sub(workspace(c, SLOT_CHIE, D, n), 0, n);
     psie = sub(workspace(c, SLOT_PSIE, D, n), 0, n);
     import_spinor(g, chi_canon, rs, 0, chie, s);
-    std::vector<double> no = norm2(c, chi), ne = norm2(c, chie);
+    src_no = norm2(c, chi);
+    src_ne = norm2(c, chie);
     if (approx_prep) {
       chio = sub(workspace(c, SLOT_CHIO, D, n), 0, n);
       blas_copy(g, chio, chi, s);
@@ -843,10 +845,10 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     }
     // the even reconstruction is exact, so the full residual equals the odd one: solve the odd
     // system to target * |chi| / |chi'_o| so that |M psi - chi| / |chi| meets the target
-    std::vector<double> np = norm2(c, chi);
+    src_np = norm2(c, chi);
     double scale = 1.0;
     for (int i = 0; i < n; ++i)
-      if (np[i] > 0) scale = std::min(scale, std::sqrt((no[i] + ne[i]) / np[i]));
+      if (src_np[i] > 0) scale = std::min(scale, std::sqrt((src_no[i] + src_ne[i]) / src_np[i]));
     p.rsd_target *= scale;
   }
   if (p.zero_guess) blas_zero(g, psi, s);
@@ -921,7 +923,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     Spinor es = sub(workspace(c, SLOT_ES, pa, n), 0, n);
     Spinor rhs = sub(workspace(c, SLOT_SE, pa, n), 0, n);
     Spinor teh = sub(workspace(c, SLOT_TEH + 50, pa, n), 0, n);
-    std::vector<double> bb = norm2(c, chi);
+    std::vector<double> bb = src_np.size() == (size_t)n ? src_np : norm2(c, chi);
     std::vector<int> done(n, 0);
     for (int i = 0; i < n; ++i)
       if (!std::isfinite(bb[i])) {
@@ -937,9 +939,10 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     // outer steps of this solve run the inner CGNE instead
     bool bicg_fallback = false;
     for (int it = 0; it <= max_outer; ++it) {
+      bool rr_is_bb = false;
       if (it == 0 && p.zero_guess) {
-        blas_copy(g, rd, chi, s);
-        blas_norm2(g, rd, red(c), s);
+        blas_copy(g, rd, chi, s);  // r = chi, |r|^2 = bb
+        rr_is_bb = true;
         rr_exact = true;
       } else if (it >= 2 && pa != D && p.system == GBC_SYS_FULL) {
         // From the third outer step on, r <- r - A e with A applied to the last correction e in
@@ -949,14 +952,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
         Spinor ta = sub(workspace(c, SLOT_XS + 50, pa, n), 0, n);
         Spinor tb = sub(workspace(c, SLOT_XS + 51, pa, n), 0, n);
         apply_sys(c, pa, mdagm, es, ta, tb, teh);
-        for (int i = 0; i < n; ++i) {
-          c->h_coef[i] = make_double2(-1.0, 0.0);
-          c->h_coef[n + i] = make_double2(1.0, 0.0);
-        }
-        GBC_CUDA(cudaMemcpyAsync(c->d_ca, c->h_coef, sizeof(double2) * n, cudaMemcpyHostToDevice, s));
-        GBC_CUDA(cudaMemcpyAsync(c->d_cb, c->h_coef + n, sizeof(double2) * n, cudaMemcpyHostToDevice, s));
-        blas_axpby(g, c->d_ca, ta, c->d_cb, rd, s);
-        blas_norm2(g, rd, red(c), s);
+        blas_xsub_norm2(g, rd, ta, red(c), s);
         rr_exact = false;
       } else if (approx_prep) {
         // r = chi_o - (A_oo psi - 1/2 D_oe A_ee^-1 (chi_e + 1/2 D_eo psi)) from the original
@@ -973,7 +969,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
         blas_xmy_norm2(g, chi, rd, red(c), s);
         rr_exact = DX == D;
       }
-      std::vector<double> rr = fetch(c, 1, n);
+      std::vector<double> rr = rr_is_bb ? bb : fetch(c, 1, n);
       // A correction that left the FP64 residual larger than before (an inner solve that broke
       // down) is taken back, and that right-hand side stops with the better iterate.
       bool revert = false;
@@ -1071,7 +1067,7 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
 
   // true FP64 residual of the system solved, then even reconstruction for the full system
   // (the full system reports the residual of M over both parities, computed below instead)
-  std::vector<double> bb = norm2(c, chi);
+  std::vector<double> bb = p.system == GBC_SYS_FULL ? std::vector<double>(n, 0.0) : norm2(c, chi);
   std::vector<double> rr(n, 0.0);
   if (p.system != GBC_SYS_FULL) {
     if (known_rr.size() == (size_t)n) {
@@ -1097,16 +1093,19 @@ int solve_device(gbc_ctx* c, const gbc_solve_params* pp, int nrhs, double* psi_c
     Spinor uo = sub(workspace(c, SLOT_T2, D, n), 0, n);
     apply_clover(c, D, 0, false, psie, ue);
     hop(c, D, 1, HOP_XPAY, false, -0.5, psie, uo, &psi, fd.clov[1], false);
-    Spinor chio = sub(workspace(c, SLOT_PSIE + 50, D, n), 0, n);
-    import_spinor(g, chi_canon, rs, 1, chio, s);
+    // the original odd source: kept from the Schur prep, else imported again
+    Spinor src_o = chio;
+    if (!approx_prep) {
+      src_o = sub(workspace(c, SLOT_PSIE + 50, D, n), 0, n);
+      import_spinor(g, chi_canon, rs, 1, src_o, s);
+    }
     blas_xmy_norm2(g, t1, ue, red(c), s);
     std::vector<double> re = fetch(c, 1, n);
-    blas_xmy_norm2(g, chio, uo, red(c), s);
+    blas_xmy_norm2(g, src_o, uo, red(c), s);
     std::vector<double> ro = fetch(c, 1, n);
-    std::vector<double> ne = norm2(c, chie), no = norm2(c, chio);
     for (int i = 0; i < n; ++i) {
       rr[i] = re[i] + ro[i];
-      bb[i] = ne[i] + no[i];
+      bb[i] = src_ne[i] + src_no[i];
     }
   }
   GBC_CUDA(cudaGetLastError());
