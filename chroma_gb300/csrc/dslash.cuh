@@ -188,6 +188,106 @@ __device__ __forceinline__ void hop_dir(cplx<typename P::real> (&acc)[12], const
   }
 }
 
+// Double-float arithmetic: the 8 hops as one rolled loop, so that the long double-float code of
+// the spin projection, the colour product and the accumulation exists once instead of 8 times
+// (the fully unrolled form stalled on instruction fetch).  Per hop only data movement depends on
+// the direction: the projection is h = p_top + w with w = s A p_bot, the accumulation
+// acc_top += uh, acc_bot += v with v = s B uh, and A, B are permutations with factors +-1, +-i;
+// a backward hop multiplies by U^dag, the conjugate transpose of the loaded link.  The operations
+// and their order are those of hop_dir, so the results are bit for bit the same.
+template <typename P, int RECON, bool DAG>
+__device__ __forceinline__ void hop_rolled_df(cplx<df64> (&acc)[12], const HopArgs& a, const Coord& c, int idx,
+                                              const char* in, const float* in_norm) {
+  const Geom& g = a.g;
+#pragma unroll 1
+  for (int hp = 0; hp < 8; ++hp) {
+    const int mu = hp >> 1;
+    const bool fwd = (hp & 1) == 0;
+    const bool neg = fwd ? !DAG : DAG;  // s = -1: forward (1 - isign gamma), backward (1 + isign gamma)
+    Coord n = c;
+    int xm = c.x[0], lm = g.L[0];
+#pragma unroll
+    for (int d = 1; d < 4; ++d)
+      if (mu == d) {
+        xm = c.x[d];
+        lm = g.L[d];
+      }
+    const int xn = fwd ? (xm + 1 == lm ? 0 : xm + 1) : (xm == 0 ? lm - 1 : xm - 1);
+#pragma unroll
+    for (int d = 0; d < 4; ++d)
+      if (mu == d) n.x[d] = xn;
+    const int ni = cb_index(g, n);
+    cplx<df64> s[12], h[2][3], uh[2][3], u[9], w0[3], w1[3];
+    load_spinor<P>(s, in, in_norm, ni, g.stride);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const cplx<df64> p2 = s[6 + k], p3 = s[9 + k];
+      if (mu == 0) {
+        w0[k] = timesI(p3);
+        w1[k] = timesI(p2);
+      } else if (mu == 1) {
+        w0[k] = -p3;
+        w1[k] = p2;
+      } else if (mu == 2) {
+        w0[k] = timesI(p2);
+        w1[k] = -timesI(p3);
+      } else {
+        w0[k] = p2;
+        w1[k] = p3;
+      }
+      if (neg) {
+        w0[k] = -w0[k];
+        w1[k] = -w1[k];
+      }
+      h[0][k] = s[k] + w0[k];
+      h[1][k] = s[3 + k] + w1[k];
+    }
+    const int tm = fwd ? c.x[3] : n.x[3];
+    const df64 sign = (mu == 3 && tm == g.L[3] - 1) ? (df64)g.t_sign : (df64)1;
+    load_link<P, RECON>(u, fwd ? a.gauge_fwd[mu] : a.gauge_bwd[mu], fwd ? idx : ni, g.stride, sign);
+    if (!fwd) {
+      // U^dag: transpose and conjugate
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int k = r + 1; k < 3; ++k) {
+          const cplx<df64> t = u[3 * r + k];
+          u[3 * r + k] = u[3 * k + r];
+          u[3 * k + r] = t;
+        }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) u[k].im = -u[k].im;
+    }
+    mat_vec2(uh, u, h);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const cplx<df64> ua = uh[0][k], ub = uh[1][k];
+      acc[k] = acc[k] + ua;
+      acc[3 + k] = acc[3 + k] + ub;
+      cplx<df64> v6, v9;
+      if (mu == 0) {
+        v6 = -timesI(ub);
+        v9 = -timesI(ua);
+      } else if (mu == 1) {
+        v6 = ub;
+        v9 = -ua;
+      } else if (mu == 2) {
+        v6 = -timesI(ua);
+        v9 = timesI(ub);
+      } else {
+        v6 = ua;
+        v9 = ub;
+      }
+      if (neg) {
+        v6 = -v6;
+        v9 = -v9;
+      }
+      acc[6 + k] = acc[6 + k] + v6;
+      acc[9 + k] = acc[9 + k] + v9;
+    }
+  }
+}
+
 // ---- FP32-arithmetic path on packed float2 instructions (FFMA2/FADD2/FMUL2 of sm_100+) ----------
 // A complex number is one float2; u*h = (ur, ur)*h + (-ui, ui)*swap(h), so every complex
 // multiply-add is two FFMA2 and every complex add one FADD2: half the instructions of scalar code.
@@ -689,6 +789,10 @@ __device__ __forceinline__ void hop_body(const HopArgs& a, int sblock, int group
       }
 #pragma unroll
       for (int k = 0; k < 12; ++k) acc[k] = {accf[k].x, accf[k].y};
+    } else if constexpr (std::is_same<T, df64>::value) {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) acc[k] = {0, 0};
+      hop_rolled_df<P, RECON, DAG>(acc, a, c, idx, in, in_norm);
     } else {
 #pragma unroll
       for (int k = 0; k < 12; ++k) acc[k] = {0, 0};
