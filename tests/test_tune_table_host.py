@@ -3,7 +3,8 @@ entry is well formed, names a shape of the compiled candidate table (kHopShapes 
 chroma_gb300/csrc/gbc_kernels.h) and carries that table's FNV-1a hash, so a change of the candidate
 shapes cannot leave a stale table behind silently (its entries would stop matching and the solves
 would fall back to timing); and it covers the stencil variants of the benchmark's propagator solve
-(FP16 12-RHS operator, FP64 and double-float outer steps on 32^3 x 64)."""
+(FP16 12-RHS operator, FP32 Schur prep and reliable updates, FP64 and double-float outer steps on
+32^3 x 64)."""
 import os
 import re
 
@@ -57,8 +58,10 @@ def test_table_covers_the_propagator_solve():
     table = entries()
     lat = [k for k in table if "|32x32x32x64|" in k]
     have = {tuple(re.search(p, k).group(1) for p in (r"prec=(\d+)", r"mode=(\d)", r"nrhs=(\d+)")) for k in lat}
+    # FP16 operator; double-float intermediate residual (PLAIN, XPAY) and M~ (CLOV); FP64
+    # reconstruction and final residual; FP32 Schur prep (PLAIN) and reliable updates (CLOV, XPAY)
     for want in [("2", "1", "12"), ("2", "2", "12"), ("16", "1", "12"), ("16", "2", "12"), ("16", "0", "12"),
-                 ("8", "0", "12"), ("8", "2", "12")]:
+                 ("8", "0", "12"), ("8", "2", "12"), ("4", "0", "12"), ("4", "1", "12"), ("4", "2", "12")]:
         assert want in have, want
     # the BiCGStab launches with fused reductions: (t, s), (t, t) and (r0, v)
     assert any("|32x32x32x64|prec=2|" in k and "|reduce=2|nrhs=12|" in k for k in lat)
