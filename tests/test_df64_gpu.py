@@ -1,5 +1,6 @@
 """Double-float arithmetic on the FP64 fields (GBC_PREC_DF64: each value hi + lo in two floats),
-the arithmetic of the solvers' Schur prep and intermediate defect-correction residuals.
+the arithmetic of the intermediate defect-correction residuals of full-system solves (and of the
+Schur prep of the solvers that iterate on it directly).
 
   - every operator block in this arithmetic against the oracle (FP64): relative error <= 1e-12
     over the output field (the same bound as the FP64 kernels; double-float carries ~48 bits),

@@ -11,6 +11,8 @@
   (clover_term_qdp_w.h:299-396 comment, makeClov :398-553) built from explicit gamma matrices.
 - Unit-gauge log det = Vh * 12 * log(4+m) (symm_prec_tests.cc:633-652).
 - LDL^dag inverse: A A^-1 = 1 on the even sites.
+- The full system's outer residual taken from the original source equals chi'_o - M~ x and the
+  odd part of chi - M psi (eoprec_fermact_qprop.cc:47-76).
 - Solvers: CG / reliable CG / FGMRES converge; the Schur-complement propagator solves the full system.
 """
 import io
@@ -241,6 +243,30 @@ def test_schur_complement_identity(orc):
     assert np.abs(full[par == 0]).max() < 1e-12
     meo = op.apply(O.OP_MEO, psi_o)
     assert np.abs(full[par == 1] - meo[par == 1]).max() < 1e-12
+
+
+def test_outer_residual_from_the_original_source(orc):
+    """The defect correction's residual of the full system, taken from the original source
+    (r = chi_o - A_oo x + 1/2 D_oe A_ee^-1 (chi_e + 1/2 D_eo x)), equals chi'_o - M~ x for the
+    Schur-prepared chi'_o = chi_o + 1/2 D_oe A_ee^-1 chi_e (eoprec_fermact_qprop.cc:47-54), and the
+    odd part of chi - M psi for psi reconstructed from x (:60-76), whose even part vanishes."""
+    dims = (4, 4, 4, 8)
+    u = orc.apply_bc(dims, orc.gauge_hot(dims, 0.3, 43))
+    op = OracleOp(dims, u, 1 / (2 * 0.124) - 4, 1.5)
+    par = parity(dims)
+    chi = rand_spinor(dims, 7)
+    chi_e, chi_o = chi * (par == 0)[:, None], chi * (par == 1)[:, None]
+    x = rand_spinor(dims, 8, cb=1)
+    chip = chi_o + 0.5 * op.apply(O.OP_DSLASH, op.apply(O.OP_CLOVER_INV, chi_e, +1, 0), +1, 1)
+    want = chip - op.apply(O.OP_MEO, x)
+    ue = op.apply(O.OP_CLOVER_INV, chi_e + 0.5 * op.apply(O.OP_DSLASH, x, +1, 0), +1, 0)
+    got = chi_o - op.apply(O.OP_CLOVER, x, +1, 1) + 0.5 * op.apply(O.OP_DSLASH, ue, +1, 1)
+    odd = par == 1
+    scale = np.abs(want[odd]).max()
+    assert np.abs(got[odd] - want[odd]).max() < 1e-13 * scale
+    full = chi - op.apply(O.OP_UNPREC, x + ue)
+    assert np.abs(full[odd] - got[odd]).max() < 1e-13 * scale
+    assert np.abs(full[par == 0]).max() < 1e-13 * scale
 
 
 def test_symmetric_operator_identities(orc):
